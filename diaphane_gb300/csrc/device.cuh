@@ -1,0 +1,76 @@
+// Device-side view of a resolved scene and the launchers shared by the
+// simulation host code (sim.cu) and the kernel translation units.
+//
+// Every kernel in this library is compiled with -fmad=false and IEEE
+// division: the update expressions are evaluated in the reference's order with
+// no multiply-add contraction, so a cell update is bit-identical to the
+// reference's f32 arithmetic (src/cpu.rs:283-434).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace diaphane {
+
+// Tables a step kernel reads.  All pointers are device pointers.
+struct DeviceScene {
+    uint32_t n[3];
+    uint64_t cells;
+    const uint8_t *material; // cells
+    const float4 *coeff;     // (electric_gain, electric_loss, magnetic_gain, magnetic_loss)
+    const float *mgain;      // nx | ny | nz, c*dt/primary width
+    const float *egain;      // nx | ny | nz, c*dt/dual width
+    const float *absorber;   // integer x|y|z, then half x|y|z
+    const float *weights;    // sheet apodization planes
+};
+
+// One injection of one step (Injection, src/source.rs:409-427).
+struct DeviceInjection {
+    uint32_t origin[3];
+    uint32_t extent[3];
+    uint32_t component;
+    uint32_t magnetic;
+    float value;
+    int32_t weight_offset; // -1: weight 1
+};
+
+// Non-silent injections of one step, in the reference's application order.
+constexpr int kMaxInjections = 32;
+struct InjectionTable {
+    uint32_t count;
+    DeviceInjection item[kMaxInjections];
+};
+
+// Fields of one buffer set: component a of E at e + a*cells.
+struct FieldSet {
+    float *e;
+    float *h;
+};
+
+// Naive path (kernels_naive.cu): one thread per cell, separate passes.
+void launch_naive_magnetic(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream);
+void launch_naive_electric(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream);
+void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj, float sign, cudaStream_t stream);
+void launch_intensity(const DeviceScene &s, const float *e, float *intensity, cudaStream_t stream);
+
+// Reductions (kernels_naive.cu).
+void launch_energy(const DeviceScene &s, FieldSet f, const float *primary, const float *dual,
+                   const float2 *eps_mu, double *partials, uint32_t blocks, cudaStream_t stream);
+void launch_finite(const DeviceScene &s, FieldSet f, int32_t *flag, cudaStream_t stream);
+uint32_t energy_blocks(uint64_t cells);
+
+// Fused path (kernels_fused.cu): one launch per step, reads `in`, writes `out`.
+struct FusedPlan {
+    uint32_t tile_y;   // rows per tile
+    uint32_t z_chunk;  // planes per work unit
+    uint32_t tiles_x, tiles_y, chunks;
+    uint32_t grid;     // CTAs launched
+    size_t smem;       // dynamic shared memory per CTA
+};
+bool fused_supported(const uint32_t n[3]);
+FusedPlan fused_plan(const uint32_t n[3], uint32_t tile_y, uint32_t z_chunk, int sm_count);
+void launch_fused_step(const DeviceScene &s, const FusedPlan &plan, FieldSet in, FieldSet out,
+                       float *intensity, const InjectionTable &table, uint32_t *work_counter,
+                       cudaStream_t stream);
+
+} // namespace diaphane

@@ -1,0 +1,220 @@
+// One-thread-per-cell kernels: the H pass, the E pass, an injection pass,
+// the intensity pass, and the energy / finiteness reductions.
+//
+// These mirror the reference step's structure (src/cpu.rs:174-198) pass for
+// pass and are kept for three jobs: the exact inverse step (reverse_by), the
+// small-grid fallback the fused kernel does not cover, and an independent
+// second implementation the fused kernel is checked against.
+#include "device.cuh"
+
+namespace diaphane {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ void decompose(uint64_t i, const uint32_t n[3], uint32_t c[3]) {
+    c[0] = uint32_t(i % n[0]);
+    uint64_t t = i / n[0];
+    c[1] = uint32_t(t % n[1]);
+    c[2] = uint32_t(t / n[1]);
+}
+
+// Absorber sample: section 0 holds integer positions, section 1 half ones.
+__device__ __forceinline__ float profile(const float *absorber, uint32_t span, const uint32_t offset[3], int axis,
+                                         uint32_t coord, bool half) {
+    return __ldg(&absorber[(half ? span : 0) + offset[axis] + coord]);
+}
+
+// update_magnetic (src/cpu.rs:283-376) and reverse_magnetic (:490-572) for
+// every cell at once: the bulk sweep and the two high-wall planes are the same
+// expression with the missing forward neighbour read as the wall's zero.
+template <bool Reverse>
+__global__ void __launch_bounds__(kThreads) magnetic_pass(DeviceScene s, const float *__restrict__ e,
+                                                          float *__restrict__ h) {
+    const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
+    if (i >= s.cells) return;
+    uint32_t c[3];
+    decompose(i, s.n, c);
+    const uint64_t stride[3] = {1, s.n[0], uint64_t(s.n[0]) * s.n[1]};
+    const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
+    const uint32_t span = s.n[0] + s.n[1] + s.n[2];
+    const float4 k = s.coeff[s.material[i]];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int b = (a + 1) % 3, cc = (a + 2) % 3;
+        const float *ec = e + uint64_t(cc) * s.cells;
+        const float *eb = e + uint64_t(b) * s.cells;
+        const float next_c = c[b] + 1 < s.n[b] ? ec[i + stride[b]] : 0.0f;
+        const float next_b = c[cc] + 1 < s.n[cc] ? eb[i + stride[cc]] : 0.0f;
+        const float curl = __ldg(&s.mgain[offset[b] + c[b]]) * (next_c - ec[i]) -
+                           __ldg(&s.mgain[offset[cc] + c[cc]]) * (next_b - eb[i]);
+        // magnetic_row: the integer profile along a, half along the others.
+        const float row = profile(s.absorber, span, offset, 1, c[1], a != 1) +
+                          profile(s.absorber, span, offset, 2, c[2], a != 2);
+        const float loss = (k.w + row) + profile(s.absorber, span, offset, 0, c[0], a != 0);
+        float *target = h + uint64_t(a) * s.cells + i;
+        const float old = *target;
+        if (Reverse)
+            *target = ((1.0f + loss) * old + k.z * curl) / (1.0f - loss);
+        else
+            *target = ((1.0f - loss) * old - k.z * curl) / (1.0f + loss);
+    }
+}
+
+// update_electric (src/cpu.rs:380-434) and reverse_electric (:441-487).
+// Index 0 along b or c is never written: the low-wall conductor.
+template <bool Reverse>
+__global__ void __launch_bounds__(kThreads) electric_pass(DeviceScene s, const float *__restrict__ h,
+                                                          float *__restrict__ e) {
+    const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
+    if (i >= s.cells) return;
+    uint32_t c[3];
+    decompose(i, s.n, c);
+    const uint64_t stride[3] = {1, s.n[0], uint64_t(s.n[0]) * s.n[1]};
+    const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
+    const uint32_t span = s.n[0] + s.n[1] + s.n[2];
+    const float4 k = s.coeff[s.material[i]];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const int b = (a + 1) % 3, cc = (a + 2) % 3;
+        if (c[b] == 0 || c[cc] == 0) continue;
+        const float *hc = h + uint64_t(cc) * s.cells;
+        const float *hb = h + uint64_t(b) * s.cells;
+        const float curl = __ldg(&s.egain[offset[b] + c[b]]) * (hc[i] - hc[i - stride[b]]) -
+                           __ldg(&s.egain[offset[cc] + c[cc]]) * (hb[i] - hb[i - stride[cc]]);
+        // electric_row: the half profile along a, integer along the others.
+        const float row = profile(s.absorber, span, offset, 1, c[1], a == 1) +
+                          profile(s.absorber, span, offset, 2, c[2], a == 2);
+        const float loss = (k.y + row) + profile(s.absorber, span, offset, 0, c[0], a == 0);
+        float *target = e + uint64_t(a) * s.cells + i;
+        const float old = *target;
+        if (Reverse)
+            *target = ((1.0f + loss) * old - k.x * curl) / (1.0f - loss);
+        else
+            *target = ((1.0f - loss) * old + k.x * curl) / (1.0f + loss);
+    }
+}
+
+// One soft injection over its box (fdtd.wgsl inject, src/cpu.rs:618-629).
+__global__ void __launch_bounds__(kThreads) inject_pass(DeviceScene s, FieldSet f, DeviceInjection inj, float sign) {
+    const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
+    const uint64_t count = uint64_t(inj.extent[0]) * inj.extent[1] * inj.extent[2];
+    if (i >= count) return;
+    const uint32_t dx = uint32_t(i % inj.extent[0]);
+    const uint64_t t = i / inj.extent[0];
+    const uint32_t dy = uint32_t(t % inj.extent[1]);
+    const uint32_t dz = uint32_t(t / inj.extent[1]);
+    const uint64_t cell = (uint64_t(inj.origin[2] + dz) * s.n[1] + (inj.origin[1] + dy)) * s.n[0] + inj.origin[0] + dx;
+    const float weight = inj.weight_offset < 0 ? 1.0f : __ldg(&s.weights[inj.weight_offset + i]);
+    float *field = (inj.magnetic ? f.h : f.e) + uint64_t(inj.component) * s.cells;
+    field[cell] += (sign * inj.value) * weight;
+}
+
+// I += Ex² + Ey² + Ez² (src/cpu.rs:186-196).
+__global__ void __launch_bounds__(kThreads) intensity_pass(DeviceScene s, const float *__restrict__ e,
+                                                           float *__restrict__ intensity) {
+    const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
+    if (i >= s.cells) return;
+    const float ex = e[i], ey = e[s.cells + i], ez = e[2 * s.cells + i];
+    float sum = ex * ex;
+    sum += ey * ey;
+    sum += ez * ez;
+    intensity[i] += sum;
+}
+
+// energy (src/cpu.rs:654-687): each component integrated over its own box,
+// accumulated in f64.  One partial pair per block; the host adds them.
+__global__ void __launch_bounds__(kThreads) energy_pass(DeviceScene s, FieldSet f, const float *__restrict__ primary,
+                                                        const float *__restrict__ dual,
+                                                        const float2 *__restrict__ eps_mu, double *partials) {
+    const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
+    double ee = 0.0, em = 0.0;
+    for (uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x; i < s.cells;
+         i += uint64_t(gridDim.x) * kThreads) {
+        uint32_t c[3];
+        decompose(i, s.n, c);
+        const float2 m = eps_mu[s.material[i]];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const int b = (a + 1) % 3, cc = (a + 2) % 3;
+            const float ev = f.e[uint64_t(a) * s.cells + i];
+            const float hv = f.h[uint64_t(a) * s.cells + i];
+            const double volume_e = double(primary[offset[a] + c[a]]) * double(dual[offset[b] + c[b]]) *
+                                    double(dual[offset[cc] + c[cc]]);
+            const double volume_h = double(dual[offset[a] + c[a]]) * double(primary[offset[b] + c[b]]) *
+                                    double(primary[offset[cc] + c[cc]]);
+            ee += 0.5 * volume_e * double(m.x * ev * ev);
+            em += 0.5 * volume_h * double(m.y * hv * hv);
+        }
+    }
+    __shared__ double se[kThreads], sm[kThreads];
+    se[threadIdx.x] = ee;
+    sm[threadIdx.x] = em;
+    __syncthreads();
+    for (int w = kThreads / 2; w > 0; w >>= 1) {
+        if (int(threadIdx.x) < w) {
+            se[threadIdx.x] += se[threadIdx.x + w];
+            sm[threadIdx.x] += sm[threadIdx.x + w];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partials[2 * blockIdx.x] = se[0];
+        partials[2 * blockIdx.x + 1] = sm[0];
+    }
+}
+
+// is_finite (src/cpu.rs:707-713): any non-finite value clears the flag.
+__global__ void __launch_bounds__(kThreads) finite_pass(DeviceScene s, FieldSet f, int32_t *flag) {
+    const uint64_t total = 3 * s.cells;
+    bool ok = true;
+    for (uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x; i < total; i += uint64_t(gridDim.x) * kThreads)
+        ok = ok && isfinite(f.e[i]) && isfinite(f.h[i]);
+    if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicExch(flag, 0);
+}
+
+uint32_t blocks_for(uint64_t n) { return uint32_t((n + kThreads - 1) / kThreads); }
+
+} // namespace
+
+void launch_naive_magnetic(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream) {
+    if (reverse)
+        magnetic_pass<true><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.e, f.h);
+    else
+        magnetic_pass<false><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.e, f.h);
+}
+
+void launch_naive_electric(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream) {
+    if (reverse)
+        electric_pass<true><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.h, f.e);
+    else
+        electric_pass<false><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.h, f.e);
+}
+
+void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj, float sign, cudaStream_t stream) {
+    const uint64_t count = uint64_t(inj.extent[0]) * inj.extent[1] * inj.extent[2];
+    if (count == 0) return;
+    inject_pass<<<blocks_for(count), kThreads, 0, stream>>>(s, f, inj, sign);
+}
+
+void launch_intensity(const DeviceScene &s, const float *e, float *intensity, cudaStream_t stream) {
+    intensity_pass<<<blocks_for(s.cells), kThreads, 0, stream>>>(s, e, intensity);
+}
+
+uint32_t energy_blocks(uint64_t cells) {
+    uint64_t b = blocks_for(cells);
+    return uint32_t(b < 1024 ? b : 1024);
+}
+
+void launch_energy(const DeviceScene &s, FieldSet f, const float *primary, const float *dual, const float2 *eps_mu,
+                   double *partials, uint32_t blocks, cudaStream_t stream) {
+    energy_pass<<<blocks, kThreads, 0, stream>>>(s, f, primary, dual, eps_mu, partials);
+}
+
+void launch_finite(const DeviceScene &s, FieldSet f, int32_t *flag, cudaStream_t stream) {
+    uint64_t b = blocks_for(3 * s.cells);
+    finite_pass<<<uint32_t(b < 2048 ? b : 2048), kThreads, 0, stream>>>(s, f, flag);
+}
+
+} // namespace diaphane

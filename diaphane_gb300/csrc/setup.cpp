@@ -1,0 +1,512 @@
+// Host-side scene resolution.  See setup.hpp.
+//
+// Arithmetic follows the reference's f32 expressions in their evaluation
+// order (Rust never contracts to FMA; this file is compiled with
+// -ffp-contract=off), so the tables uploaded to the device are the ones the
+// reference's own solvers would hold.
+#include "setup.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+namespace diaphane {
+
+namespace {
+
+[[noreturn]] void invalid(const std::string &m) { throw Error(DP_ERR_INVALID, m); }
+
+// Rust `as` casts from f32 saturate at the target range.
+size_t to_index(float v) {
+    if (!(v > 0.0f)) return 0;
+    if (v >= 1.8446744e19f) return SIZE_MAX;
+    return size_t(v);
+}
+uint32_t to_u32(float v) {
+    if (!(v > 0.0f)) return 0;
+    if (v >= 4294967296.0f) return UINT32_MAX;
+    return uint32_t(v);
+}
+
+Axis1D assemble(std::vector<float> primary, std::vector<float> corners) {
+    // Spacing::assemble, src/grid.rs:192-214.
+    if (primary.size() < 2) invalid("an axis needs at least 2 cells");
+    for (float w : primary)
+        if (!(w > 0.0f && std::isfinite(w))) invalid("cell widths must be positive and finite");
+    Axis1D axis;
+    axis.dual.resize(primary.size());
+    axis.dual[0] = 0.5f * (primary[0] + primary[0]);
+    for (size_t i = 1; i < primary.size(); ++i) axis.dual[i] = 0.5f * (primary[i - 1] + primary[i]);
+    axis.primary = std::move(primary);
+    axis.corners = std::move(corners);
+    return axis;
+}
+
+} // namespace
+
+float Axis1D::finest() const {
+    float m = std::numeric_limits<float>::infinity();
+    for (float w : primary) m = std::fmin(m, w);
+    return m;
+}
+
+float Axis1D::coarsest() const {
+    float m = -std::numeric_limits<float>::infinity();
+    for (float w : primary) m = std::fmax(m, w);
+    return m;
+}
+
+float Axis1D::worst_ratio() const {
+    float m = 1.0f;
+    for (size_t i = 1; i < primary.size(); ++i)
+        m = std::fmax(m, std::fmax(primary[i] / primary[i - 1], primary[i - 1] / primary[i]));
+    return m;
+}
+
+// Spacing::position / offset_of, src/grid.rs:262-285.
+float Axis1D::position(float coordinate) const {
+    size_t last = primary.size() - 1;
+    size_t i = std::min(to_index(std::fmax(std::floor(coordinate), 0.0f)), last);
+    float offset = corners[i] + (coordinate - float(i)) * primary[i];
+    return offset - 0.5f * length();
+}
+
+// Spacing::coordinate, src/grid.rs:269-279: a search, not a division.
+float Axis1D::coordinate(float position) const {
+    float offset = position + 0.5f * length();
+    size_t first_past = size_t(std::upper_bound(corners.begin(), corners.end(), offset) - corners.begin());
+    size_t i = first_past == 0 ? 0 : first_past - 1;
+    if (i > primary.size() - 1) i = primary.size() - 1;
+    return float(i) + (offset - corners[i]) / primary[i];
+}
+
+// Spacing::uniform, src/grid.rs:167-178: corners by f64 multiplication.
+Axis1D axis_uniform(uint32_t count, float width) {
+    if (count < 2) invalid("an axis needs at least 2 cells");
+    std::vector<float> corners(size_t(count) + 1);
+    for (uint32_t i = 0; i <= count; ++i) corners[i] = float(double(i) * double(width));
+    return assemble(std::vector<float>(count, width), std::move(corners));
+}
+
+// Spacing::from_widths, src/grid.rs:181-190: corners by an f64 running sum.
+Axis1D axis_from_widths(std::vector<float> widths) {
+    std::vector<float> corners(widths.size() + 1);
+    double sum = 0.0;
+    corners[0] = 0.0f;
+    for (size_t i = 0; i < widths.size(); ++i) {
+        sum += double(widths[i]);
+        corners[i + 1] = float(sum);
+    }
+    return assemble(std::move(widths), std::move(corners));
+}
+
+// grade(), src/grid.rs:791-888: sample the target width, cap its slope with a
+// forward and a backward sweep, march the cells, re-cap them, drop the last
+// cell if that lands nearer the wall, then rescale onto the wall.
+Axis1D axis_graded(int axis, float length, float base, const dp_refinement *refinements,
+                   uint32_t refinement_count, float max_ratio) {
+    std::vector<const dp_refinement *> active;
+    for (uint32_t i = 0; i < refinement_count; ++i)
+        if (refinements[i].size[axis] > 0.0f) active.push_back(&refinements[i]);
+    if (active.empty()) return axis_uniform(to_u32(std::fmax(std::round(length / base), 2.0f)), base);
+
+    float finest = base;
+    for (const dp_refinement *r : active) finest = std::fmin(finest, r->cell_size);
+    if (!(finest > 0.0f && std::isfinite(finest))) invalid("refinement cell sizes must be positive and finite");
+
+    size_t samples = to_index(std::ceil(length / finest * 4.0f));
+    samples = std::max<size_t>(64, std::min<size_t>(samples, size_t(1) << 20));
+    const float step = length / float(samples);
+
+    std::vector<float> target(samples + 1);
+    for (size_t i = 0; i <= samples; ++i) {
+        float position = float(i) * step - 0.5f * length;
+        float width = base;
+        for (const dp_refinement *r : active) {
+            float half = 0.5f * r->size[axis];
+            if (std::fabs(position - r->center[axis]) <= half) width = std::fmin(width, r->cell_size);
+        }
+        target[i] = width;
+    }
+    const float slope = (max_ratio - 1.0f) * step;
+    for (size_t i = 1; i <= samples; ++i) target[i] = std::fmin(target[i], target[i - 1] + slope);
+    for (size_t i = samples; i-- > 0;) target[i] = std::fmin(target[i], target[i + 1] + slope);
+
+    std::vector<float> widths;
+    for (float offset = 0.0f; offset < length;) {
+        size_t i = std::min(to_index(offset / step), samples);
+        widths.push_back(target[i]);
+        offset += target[i];
+        if (widths.size() > (size_t(1) << 16)) invalid("grading ran to more cells than an axis can carry");
+    }
+    for (size_t i = 1; i < widths.size(); ++i) widths[i] = std::fmin(widths[i], widths[i - 1] * max_ratio);
+    for (size_t i = widths.size() - 1; i-- > 0;) widths[i] = std::fmin(widths[i], widths[i + 1] * max_ratio);
+
+    float total = 0.0f;
+    for (float w : widths) total += w;
+    if (widths.size() > 2) {
+        float without = total - widths.back();
+        if (std::fabs(length - without) < std::fabs(total - length)) {
+            widths.pop_back();
+            total = without;
+        }
+    }
+    const float scale = length / total;
+    for (float &w : widths) w *= scale;
+    return axis_from_widths(std::move(widths));
+}
+
+// Grid::build, src/grid.rs:466-508.
+ResolvedGrid ResolvedGrid::build(const dp_grid_spec &spec) {
+    if (!(spec.cell_size > 0.0f && std::isfinite(spec.cell_size))) invalid("cell size must be positive and finite");
+    if (!(spec.max_ratio > 1.0f && std::isfinite(spec.max_ratio))) invalid("the growth cap must exceed 1");
+    if (spec.refinement_count > 0 && spec.refinements == nullptr) invalid("refinements pointer is null");
+    ResolvedGrid g;
+    for (int a = 0; a < 3; ++a) {
+        if (spec.refinement_count == 0)
+            g.axes[a] = axis_uniform(spec.extent[a], spec.cell_size);
+        else
+            g.axes[a] = axis_graded(a, float(spec.extent[a]) * spec.cell_size, spec.cell_size, spec.refinements,
+                                    spec.refinement_count, spec.max_ratio);
+        g.n[a] = uint32_t(g.axes[a].primary.size());
+    }
+    g.courant = spec.courant;
+    return g;
+}
+
+// Grid::validate, src/grid.rs:747-773.
+void ResolvedGrid::validate() const {
+    for (int a = 0; a < 3; ++a)
+        if (n[a] < 2) invalid("grid must be at least 2 cells across on every axis");
+    if (!(courant > 0.0f && courant <= kCourantLimit)) invalid("Courant number is outside (0, 1/sqrt(3)]; the scheme would diverge");
+}
+
+// src/grid.rs:575-584.
+float ResolvedGrid::reference_cell_size() const {
+    float inverse_squares = 0.0f;
+    for (int a = 0; a < 3; ++a) {
+        float f = axes[a].finest();
+        inverse_squares += 1.0f / (f * f);
+    }
+    return std::sqrt(3.0f / inverse_squares);
+}
+
+float ResolvedGrid::time_step() const { return courant * reference_cell_size() / kSpeedOfLight; }
+
+float ResolvedGrid::finest() const {
+    float m = std::numeric_limits<float>::infinity();
+    for (int a = 0; a < 3; ++a) m = std::fmin(m, axes[a].finest());
+    return m;
+}
+
+float ResolvedGrid::coarsest() const {
+    float m = -std::numeric_limits<float>::infinity();
+    for (int a = 0; a < 3; ++a) m = std::fmax(m, axes[a].coarsest());
+    return m;
+}
+
+void ResolvedGrid::cell_center(const uint32_t coord[3], float out[3]) const {
+    for (int a = 0; a < 3; ++a) out[a] = axes[a].position(float(coord[a]) + 0.5f);
+}
+
+void ResolvedGrid::cell_containing(const float position[3], uint32_t out[3]) const {
+    for (int a = 0; a < 3; ++a) {
+        float c = axes[a].coordinate(position[a]);
+        size_t i = to_index(std::fmax(std::floor(c), 0.0f));
+        out[a] = uint32_t(std::min<size_t>(i, n[a] - 1));
+    }
+}
+
+bool ResolvedGrid::contains(const float position[3]) const {
+    for (int a = 0; a < 3; ++a)
+        if (!(std::fabs(position[a]) <= 0.5f * axes[a].length())) return false;
+    return true;
+}
+
+// Waveform::evaluate, src/source.rs:74-115.
+float waveform_value(const dp_waveform &w, float t) {
+    switch (w.kind) {
+    case DP_WAVE_RICKER: {
+        float arg = kPi * w.frequency * (t - w.delay);
+        float arg2 = arg * arg;
+        return (1.0f - 2.0f * arg2) * std::exp(-arg2);
+    }
+    case DP_WAVE_GAUSSIAN_PULSE: {
+        const float fwhm_to_sigma = 0.4246609f; // 1 / (2 sqrt(2 ln 2))
+        float sigma = fwhm_to_sigma * w.duration_cycles / w.frequency;
+        float tau = t - w.delay;
+        float envelope = std::exp(-0.5f * (tau / sigma) * (tau / sigma));
+        return envelope * std::sin(2.0f * kPi * w.frequency * tau);
+    }
+    case DP_WAVE_CONTINUOUS: {
+        if (t <= 0.0f) return 0.0f;
+        float ramp = w.ramp_cycles / w.frequency;
+        float envelope = t >= ramp ? 1.0f : 0.5f * (1.0f - std::cos(kPi * t / ramp));
+        return envelope * std::sin(2.0f * kPi * w.frequency * t);
+    }
+    }
+    return 0.0f;
+}
+
+// Injection::weight, src/source.rs:441-455.
+float injection_weight(const StepInjection &inj, const float position[3]) {
+    if (inj.inverse_waist_squared == 0.0f) return 1.0f;
+    float r2 = 0.0f;
+    for (int a = 0; a < 3; ++a)
+        if (inj.extent[a] > 1) {
+            float d = position[a] - inj.center[a];
+            r2 += d * d;
+        }
+    return std::exp(-r2 * inj.inverse_waist_squared);
+}
+
+namespace {
+
+// Material::coefficients, src/material.rs:100-122.
+Coeff material_coefficients(const dp_material &m, float dt) {
+    if (std::isinf(m.conductivity)) return Coeff{0.0f, 1.0f, 1.0f / m.relative_permeability, 0.0f};
+    float half_step = 0.5f * dt;
+    return Coeff{1.0f / m.relative_permittivity,
+                 half_step * m.conductivity / (kVacuumPermittivity * m.relative_permittivity),
+                 1.0f / m.relative_permeability,
+                 half_step * m.magnetic_loss / (kVacuumPermeability * m.relative_permeability)};
+}
+
+// Shape::contains, src/scene.rs:60-81.
+bool shape_contains(const dp_shape &s, const float p[3]) {
+    if (s.kind == DP_SHAPE_BLOCK) {
+        for (int a = 0; a < 3; ++a)
+            if (!(std::fabs(p[a] - s.center[a]) <= 0.5f * s.size[a])) return false;
+        return true;
+    }
+    if (s.kind == DP_SHAPE_SPHERE) {
+        float d0 = p[0] - s.center[0], d1 = p[1] - s.center[1], d2 = p[2] - s.center[2];
+        float r2 = d0 * d0;
+        r2 += d1 * d1;
+        r2 += d2 * d2;
+        return r2 <= s.radius * s.radius;
+    }
+    return std::fabs(p[s.axis] - s.offset) <= 0.5f * s.thickness;
+}
+
+// Cells a shape can possibly cover along one axis: the cells containing its
+// two extremes, widened by two cells against rounding.  The exact membership
+// test runs on every cell in the range, so this only skips cells whose
+// centres lie well outside the shape (Shape::bounds, src/scene.rs:85-102).
+void shape_range(const ResolvedGrid &g, const dp_shape &s, int a, uint32_t &lo, uint32_t &hi) {
+    float center = 0.0f, half = std::numeric_limits<float>::infinity();
+    if (s.kind == DP_SHAPE_BLOCK) {
+        center = s.center[a];
+        half = 0.5f * std::fabs(s.size[a]);
+    } else if (s.kind == DP_SHAPE_SPHERE) {
+        center = s.center[a];
+        half = std::fabs(s.radius);
+    } else if (int(s.axis) == a) {
+        center = s.offset;
+        half = 0.5f * std::fabs(s.thickness);
+    }
+    lo = 0;
+    hi = g.n[a] - 1;
+    if (!std::isfinite(half) || !std::isfinite(center)) return;
+    float c_lo = g.axes[a].coordinate(center - half), c_hi = g.axes[a].coordinate(center + half);
+    long l = long(std::floor(c_lo)) - 2, h = long(std::floor(c_hi)) + 2;
+    if (h < 0 || l > long(g.n[a]) - 1) {
+        lo = 1;
+        hi = 0; // empty
+        return;
+    }
+    lo = uint32_t(std::max<long>(l, 0));
+    hi = uint32_t(std::min<long>(h, long(g.n[a]) - 1));
+}
+
+} // namespace
+
+Scene Scene::build(const dp_scene_desc &d) {
+    Scene s;
+    s.grid = ResolvedGrid::build(d.grid);
+    s.grid.validate();
+    s.boundary = d.boundary;
+    if (d.material_count == 0 || d.materials == nullptr) invalid("a material table needs vacuum at index 0");
+    if (d.material_count > 256) throw Error(DP_ERR_UNSUPPORTED, "at most 256 materials: the material index is stored as u8");
+    if ((d.shape_count && !d.shapes) || (d.source_count && !d.sources)) invalid("null shape or source array");
+    s.materials.assign(d.materials, d.materials + d.material_count);
+    s.shapes.assign(d.shapes, d.shapes + d.shape_count);
+    s.sources.assign(d.sources, d.sources + d.source_count);
+    for (const auto &sh : s.shapes)
+        if (sh.material >= d.material_count) invalid("a shape refers to a material outside the table");
+    for (const auto &src : s.sources) {
+        if (src.polarization > 2 || src.axis > 2) invalid("an axis index must be 0, 1 or 2");
+        if (src.shape > DP_SOURCE_PLANE_WAVE || src.waveform.kind > DP_WAVE_CONTINUOUS) invalid("unknown source or waveform kind");
+    }
+
+    const ResolvedGrid &g = s.grid;
+    s.dt = g.time_step();
+
+    // Grid::magnetic_gains / electric_gains, src/grid.rs:602-613.
+    const float travel = kSpeedOfLight * s.dt;
+    for (int a = 0; a < 3; ++a) {
+        for (float w : g.axes[a].primary) s.magnetic_gains.push_back(travel / w);
+        for (float w : g.axes[a].dual) s.electric_gains.push_back(travel / w);
+        for (uint32_t i = 0; i < g.n[a]; ++i) s.centers.push_back(g.axes[a].position(float(i) + 0.5f));
+        s.primary.insert(s.primary.end(), g.axes[a].primary.begin(), g.axes[a].primary.end());
+        s.dual.insert(s.dual.end(), g.axes[a].dual.begin(), g.axes[a].dual.end());
+    }
+
+    // MaterialTable::coefficients, src/material.rs:207-212.
+    for (const auto &m : s.materials) s.coefficients.push_back(material_coefficients(m, s.dt));
+
+    // AbsorbingProfile::new, src/boundary.rs:100-145.
+    const uint32_t span = g.n[0] + g.n[1] + g.n[2];
+    s.absorber.assign(2 * size_t(span), 0.0f);
+    uint32_t thickness = d.boundary.kind == DP_BOUNDARY_ABSORBING ? d.boundary.thickness : 0;
+    if (d.boundary.kind != DP_BOUNDARY_PEC && d.boundary.kind != DP_BOUNDARY_ABSORBING) invalid("unknown boundary kind");
+    if (thickness > 0) {
+        for (int a = 0; a < 3; ++a)
+            if (!(2 * size_t(thickness) < g.n[a])) invalid("absorbing layers do not fit in the axis");
+        float target = d.boundary.target_reflection;
+        if (!(target > 0.0f && target < 1.0f)) invalid("target reflection must lie in (0, 1)");
+        const float order = 3.0f;
+        const float t = float(thickness);
+        const float peak = -(order + 1.0f) * std::log(target) * g.courant / (4.0f * t);
+        for (int a = 0; a < 3; ++a) {
+            const float outer = float(g.n[a] - 1);
+            for (uint32_t i = 0; i < g.n[a]; ++i) {
+                for (int h = 0; h < 2; ++h) {
+                    float position = h ? float(i) + 0.5f : float(i);
+                    float depth = std::fmax((t - position) / t, (t - (outer - position)) / t);
+                    depth = depth < 0.0f ? 0.0f : (depth > 1.0f ? 1.0f : depth);
+                    s.absorber[size_t(h) * span + s.axis_offset(a) + i] = peak * std::pow(depth, order);
+                }
+            }
+        }
+    }
+    for (float v : s.absorber) s.absorber_peak = std::fmax(s.absorber_peak, v);
+
+    // is_reversible, src/cpu.rs:209-215.
+    s.reversible = s.absorber_peak == 0.0f;
+    for (const Coeff &c : s.coefficients)
+        if (!(c.electric_loss == 0.0f && c.magnetic_loss == 0.0f)) s.reversible = false;
+
+    // Scene::material_indices, src/scene.rs:181-206: later shapes overwrite
+    // earlier ones, membership decided at the cell centre.
+    const uint64_t cells = g.cells();
+    s.material_index.assign(cells, 0);
+    for (const dp_shape &sh : s.shapes) {
+        uint32_t lo[3], hi[3];
+        bool empty = false;
+        for (int a = 0; a < 3; ++a) {
+            shape_range(g, sh, a, lo[a], hi[a]);
+            if (lo[a] > hi[a]) empty = true;
+        }
+        if (empty) continue;
+        const uint8_t material = uint8_t(sh.material);
+        const long z0 = lo[2], z1 = hi[2];
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long z = z0; z <= z1; ++z) {
+            float p[3];
+            p[2] = s.centers[s.axis_offset(2) + uint32_t(z)];
+            for (uint32_t y = lo[1]; y <= hi[1]; ++y) {
+                p[1] = s.centers[s.axis_offset(1) + y];
+                uint8_t *row = &s.material_index[(uint64_t(z) * g.n[1] + y) * g.n[0]];
+                for (uint32_t x = lo[0]; x <= hi[0]; ++x) {
+                    p[0] = s.centers[x];
+                    if (shape_contains(sh, p)) row[x] = material;
+                }
+            }
+        }
+    }
+
+    // Sheet apodization planes (src/source.rs:304-333 with the weight of
+    // src/source.rs:441-455), evaluated once per sheet.
+    s.source_weight.assign(s.sources.size(), -1);
+    std::vector<StepInjection> probe;
+    for (size_t k = 0; k < s.sources.size(); ++k) {
+        const dp_source &src = s.sources[k];
+        if (src.shape != DP_SOURCE_SHEET) continue;
+        s.injections(0.0f, probe); // the box does not depend on time
+        const StepInjection &inj = probe[2 * k];
+        s.source_weight[k] = int32_t(s.weights.size());
+        for (uint32_t dz = 0; dz < inj.extent[2]; ++dz)
+            for (uint32_t dy = 0; dy < inj.extent[1]; ++dy)
+                for (uint32_t dx = 0; dx < inj.extent[0]; ++dx) {
+                    uint32_t coord[3] = {inj.origin[0] + dx, inj.origin[1] + dy, inj.origin[2] + dz};
+                    float position[3];
+                    g.cell_center(coord, position);
+                    s.weights.push_back(injection_weight(inj, position));
+                }
+    }
+    return s;
+}
+
+// Source::injections, src/source.rs:280-403: two slots per source.
+void Scene::injections(float time, std::vector<StepInjection> &out) const {
+    out.clear();
+    const ResolvedGrid &g = grid;
+    for (size_t k = 0; k < sources.size(); ++k) {
+        const dp_source &src = sources[k];
+        const float value = src.amplitude * waveform_value(src.waveform, time);
+        StepInjection a{}, b{};
+        a.weight_offset = b.weight_offset = -1;
+        a.component = b.component = src.polarization;
+        if (src.shape == DP_SOURCE_POINT) {
+            float position[3];
+            for (int i = 0; i < 3; ++i) position[i] = src.at[i] + src.velocity[i] * time;
+            g.cell_containing(position, a.origin);
+            a.extent[0] = a.extent[1] = a.extent[2] = 1;
+            // A mover outside the domain is silent, not clamped.
+            a.value = g.contains(position) ? value : 0.0f;
+            b = a;
+            b.value = 0.0f;
+        } else if (src.shape == DP_SOURCE_SHEET) {
+            const int axis = int(src.axis);
+            float position[3] = {0.0f, 0.0f, 0.0f};
+            position[axis] = src.offset;
+            uint32_t cell[3];
+            g.cell_containing(position, cell);
+            for (int i = 0; i < 3; ++i) {
+                a.origin[i] = 0;
+                a.extent[i] = g.n[i];
+            }
+            a.origin[axis] = cell[axis];
+            a.extent[axis] = 1;
+            a.inverse_waist_squared = 1.0f / (src.waist * src.waist);
+            a.weight_offset = source_weight.empty() ? -1 : source_weight[k];
+            a.value = value;
+            b = a;
+            b.value = 0.0f;
+        } else {
+            // Total-field / scattered-field plane, src/source.rs:334-401.
+            const int travel = int(src.axis);
+            float position[3] = {0.0f, 0.0f, 0.0f};
+            position[travel] = src.offset;
+            uint32_t cell[3];
+            g.cell_containing(position, cell);
+            const uint32_t plane = std::max<uint32_t>(cell[travel], 1);
+            const float spacing = g.axes[travel].finest();
+            const float dt_local = g.time_step();
+            const float gain = kSpeedOfLight * dt_local / spacing;
+            const float omega = 2.0f * kPi * src.waveform.frequency;
+            const float half_k_spacing = std::asin(std::sin(0.5f * omega * dt_local) / gain);
+            const float retard = half_k_spacing / omega;
+            const int pol = int(src.polarization);
+            const uint32_t h_axis = uint32_t(3 - travel - pol);
+            const float h_sign = ((pol + 1) % 3) == travel ? -1.0f : 1.0f;
+            for (int i = 0; i < 3; ++i) {
+                a.extent[i] = b.extent[i] = g.n[i];
+            }
+            a.origin[travel] = plane;
+            a.extent[travel] = 1;
+            b.origin[travel] = plane - 1;
+            b.extent[travel] = 1;
+            a.value = gain * (src.amplitude * waveform_value(src.waveform, time - 0.5f * dt_local + retard));
+            b.component = h_axis;
+            b.magnetic = 1;
+            b.value = h_sign * gain * (src.amplitude * waveform_value(src.waveform, time - dt_local));
+        }
+        out.push_back(a);
+        out.push_back(b);
+    }
+}
+
+} // namespace diaphane

@@ -1,0 +1,117 @@
+// Host-side scene resolution: grid spacing, time step, gains, material
+// coefficients, absorbing profile, rasterized material index and per-step
+// source injections.  Everything the reference's Simulation::new computes on
+// the CPU before uploading (src/cpu.rs:100-120, src/gpu.rs:190-319), in f32
+// with the reference's operation order so device tables match it bit for bit.
+#pragma once
+
+#include "../../include/diaphane_gb300.h"
+
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+namespace diaphane {
+
+// Raised where the reference panics; the C ABI turns it into a status.
+struct Error : std::runtime_error {
+    dp_status status;
+    Error(dp_status s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+constexpr float kSpeedOfLight = 299792458.0f;
+constexpr float kVacuumPermeability = 1.2566371e-6f;
+constexpr float kVacuumPermittivity = 8.854188e-12f;
+constexpr float kCourantLimit = 0.57735026f;
+constexpr float kPi = 3.14159265358979323846f;
+
+// Cell widths of one axis (Spacing, src/grid.rs:149-286).
+struct Axis1D {
+    std::vector<float> primary; // corner i to corner i+1
+    std::vector<float> dual;    // centre i-1 to centre i
+    std::vector<float> corners; // primary.size() + 1 offsets from the low wall
+
+    float length() const { return corners.back(); }
+    float finest() const;
+    float coarsest() const;
+    float worst_ratio() const;
+    float position(float coordinate) const;   // cell coordinate -> metres from the centre
+    float coordinate(float position) const;   // metres from the centre -> cell coordinate
+};
+
+Axis1D axis_uniform(uint32_t count, float width);
+Axis1D axis_from_widths(std::vector<float> widths);
+Axis1D axis_graded(int axis, float length, float base, const dp_refinement *refinements,
+                   uint32_t refinement_count, float max_ratio);
+
+struct ResolvedGrid {
+    uint32_t n[3];
+    float courant;
+    Axis1D axes[3];
+
+    static ResolvedGrid build(const dp_grid_spec &spec);
+    void validate() const;
+    uint64_t cells() const { return uint64_t(n[0]) * n[1] * n[2]; }
+    float reference_cell_size() const;
+    float time_step() const;
+    float finest() const;
+    float coarsest() const;
+    void cell_center(const uint32_t coord[3], float out[3]) const;
+    void cell_containing(const float position[3], uint32_t out[3]) const;
+    bool contains(const float position[3]) const;
+};
+
+struct Coeff {
+    float electric_gain, electric_loss, magnetic_gain, magnetic_loss;
+};
+
+// One injection slot for one step, ready for a kernel.
+struct StepInjection {
+    uint32_t origin[3];
+    uint32_t extent[3];
+    uint32_t component;
+    uint32_t magnetic;
+    float value;
+    int32_t weight_offset; // into Scene::weights, -1 when every cell weighs 1
+    float inverse_waist_squared;
+    float center[3];
+};
+
+// The resolved scene: the tables the kernels read.
+struct Scene {
+    ResolvedGrid grid;
+    dp_boundary boundary;
+    std::vector<dp_material> materials;
+    std::vector<dp_shape> shapes;
+    std::vector<dp_source> sources;
+
+    std::vector<float> magnetic_gains; // nx | ny | nz
+    std::vector<float> electric_gains; // nx | ny | nz
+    std::vector<float> centers;        // nx | ny | nz
+    std::vector<float> primary;        // nx | ny | nz
+    std::vector<float> dual;           // nx | ny | nz
+    std::vector<float> absorber;       // integer x|y|z then half x|y|z
+    std::vector<Coeff> coefficients;
+    std::vector<uint8_t> material_index;
+    float absorber_peak = 0.0f;
+    bool reversible = false;
+    float dt = 0.0f;
+
+    // Apodization weights, precomputed once per sheet source: a sheet's box
+    // never moves, so its weights never change.  source_weight[s] is the
+    // offset of source s's plane, or -1.
+    std::vector<float> weights;
+    std::vector<int32_t> source_weight;
+
+    static Scene build(const dp_scene_desc &desc);
+    uint32_t axis_offset(int axis) const { return axis == 0 ? 0 : (axis == 1 ? grid.n[0] : grid.n[0] + grid.n[1]); }
+
+    // Source::injections for every source at `time`, two slots per source.
+    void injections(float time, std::vector<StepInjection> &out) const;
+};
+
+float waveform_value(const dp_waveform &w, float time);
+float injection_weight(const StepInjection &inj, const float position[3]);
+
+} // namespace diaphane

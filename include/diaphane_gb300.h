@@ -1,0 +1,299 @@
+/*
+ * diaphane_gb300 — C ABI of a GB300-native (sm_103a) Yee leapfrog time step.
+ *
+ * This is the drop-in boundary for the step / source-injection / field
+ * read-back API that the reference's two solvers share (src/cpu.rs:97-714 and
+ * src/gpu.rs:180-730, trait Steppable in src/timeline.rs:63-72).  Every entry
+ * point below names the reference interface it replaces.
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  The caller owns every host buffer it
+ *     passes; the library owns the device buffers behind a handle.
+ *   - Errors come back as dp_status codes where the reference panics
+ *     (assert!/expect).  dp_last_error() returns a message for the calling
+ *     thread.
+ *   - One handle is used from one thread at a time.  Each simulation owns one
+ *     CUDA stream; dp_sim_advance and dp_sim_reverse are asynchronous on it,
+ *     exactly as gpu::Simulation::advance_by returns after submit.  Reads wait.
+ *   - Fields are component-major and x-major inside a component: component a
+ *     of a field occupies [a*cells, (a+1)*cells), cell (x,y,z) sits at
+ *     (z*ny + y)*nx + x (src/grid.rs:119-126, src/gpu.rs:25-30).
+ *   - There is no CPU fallback: every dp_sim_* call runs on the GPU and fails
+ *     with DP_ERR_CUDA when no device is usable.
+ */
+#ifndef DIAPHANE_GB300_H
+#define DIAPHANE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------ */
+/* Status                                                                   */
+/* ------------------------------------------------------------------------ */
+
+typedef enum dp_status {
+    DP_OK = 0,
+    DP_ERR_INVALID = 1,     /* a scene or argument the reference would panic on */
+    DP_ERR_LOSSY = 2,       /* reverse on a lossy scene (src/cpu.rs:253-260) */
+    DP_ERR_CUDA = 3,        /* a CUDA runtime or driver call failed */
+    DP_ERR_TIMEOUT = 4,     /* dp_sim_wait deadline passed (src/gpu.rs:616-622) */
+    DP_ERR_OOM = 5,         /* device memory or an admission budget exhausted */
+    DP_ERR_UNSUPPORTED = 6, /* a scene outside this build's limits */
+    DP_ERR_RANGE = 7,       /* step past the start, size mismatch, bad index */
+    DP_ERR_BUSY = 8         /* a request slot or arena region is in use */
+} dp_status;
+
+/* Message for the last error on the calling thread ("" when none). */
+const char *dp_last_error(void);
+const char *dp_status_string(dp_status status);
+
+/* ------------------------------------------------------------------------ */
+/* Scene recipe — flat C mirror of Scene (src/scene.rs:116-122)              */
+/* ------------------------------------------------------------------------ */
+
+enum { DP_AXIS_X = 0, DP_AXIS_Y = 1, DP_AXIS_Z = 2 };
+
+/* Refinement (src/grid.rs:313-320): metres from the domain centre. */
+typedef struct dp_refinement {
+    float center[3];
+    float size[3]; /* non-positive: that axis is not refined */
+    float cell_size;
+} dp_refinement;
+
+/* GridSpec (src/grid.rs:381-392): the recipe, not the resolved arrays. */
+typedef struct dp_grid_spec {
+    uint32_t extent[3]; /* cells at cell_size; refinements only subdivide */
+    float cell_size;    /* metres */
+    float courant;      /* S = c*dt/d_ref, in (0, 1/sqrt(3)] */
+    float max_ratio;    /* growth cap between neighbouring cells, > 1 */
+    uint32_t refinement_count;
+    const dp_refinement *refinements;
+} dp_grid_spec;
+
+enum { DP_BOUNDARY_PEC = 0, DP_BOUNDARY_ABSORBING = 1 };
+
+/* Boundary (src/boundary.rs:53-67). */
+typedef struct dp_boundary {
+    uint32_t kind;
+    uint32_t thickness;      /* cells, absorbing only */
+    float target_reflection; /* absorbing only, in (0, 1) */
+} dp_boundary;
+
+/* Material (src/material.rs:29-39).  Infinite conductivity is a PEC. */
+typedef struct dp_material {
+    float relative_permittivity;
+    float relative_permeability;
+    float conductivity;
+    float magnetic_loss;
+} dp_material;
+
+enum { DP_SHAPE_BLOCK = 0, DP_SHAPE_SPHERE = 1, DP_SHAPE_SLAB = 2 };
+
+/* Shape (src/scene.rs:32-56).  Later shapes overwrite earlier ones. */
+typedef struct dp_shape {
+    uint32_t kind;
+    uint32_t material; /* index into dp_scene_desc.materials */
+    float center[3];   /* block, sphere */
+    float size[3];     /* block: full side lengths */
+    float radius;      /* sphere */
+    uint32_t axis;     /* slab */
+    float offset;      /* slab */
+    float thickness;   /* slab */
+} dp_shape;
+
+enum { DP_WAVE_RICKER = 0, DP_WAVE_GAUSSIAN_PULSE = 1, DP_WAVE_CONTINUOUS = 2 };
+
+/* Waveform (src/source.rs:31-52). */
+typedef struct dp_waveform {
+    uint32_t kind;
+    float frequency;       /* peak (Ricker), centre (Gaussian), carrier (CW) */
+    float duration_cycles; /* Gaussian: envelope FWHM in carrier periods */
+    float ramp_cycles;     /* CW */
+    float delay;           /* Ricker, Gaussian: seconds */
+} dp_waveform;
+
+enum { DP_SOURCE_POINT = 0, DP_SOURCE_SHEET = 1, DP_SOURCE_PLANE_WAVE = 2 };
+
+/* Source (src/source.rs:136-195). */
+typedef struct dp_source {
+    uint32_t shape;
+    uint32_t polarization; /* driven E component */
+    float at[3];           /* point: metres from the domain centre */
+    float velocity[3];     /* point: metres per second */
+    uint32_t axis;         /* sheet, plane wave */
+    float offset;          /* sheet, plane wave: metres along axis */
+    float waist;           /* sheet: metres */
+    float amplitude;
+    dp_waveform waveform;
+} dp_source;
+
+/* Scene (src/scene.rs:116-122).  materials[0] must be vacuum
+ * (MaterialTable invariant, src/material.rs:160-176). */
+typedef struct dp_scene_desc {
+    dp_grid_spec grid;
+    dp_boundary boundary;
+    uint32_t material_count;
+    const dp_material *materials;
+    uint32_t shape_count;
+    const dp_shape *shapes;
+    uint32_t source_count;
+    const dp_source *sources;
+} dp_scene_desc;
+
+/* ------------------------------------------------------------------------ */
+/* Grid queries (host only): what a scene author reads off a Grid            */
+/* ------------------------------------------------------------------------ */
+
+typedef struct dp_grid_info {
+    uint32_t extent[3];        /* resolved cell counts (graded axes differ) */
+    float size[3];             /* Grid::size, src/grid.rs:587-589 */
+    float time_step;           /* Grid::time_step, src/grid.rs:592-594 */
+    float finest;              /* Grid::finest, src/grid.rs:554-559 */
+    float coarsest;            /* Grid::coarsest, src/grid.rs:561-566 */
+    float worst_ratio;         /* Grid::worst_ratio, src/grid.rs:541-546 */
+    float reference_cell_size; /* src/grid.rs:575-584 */
+} dp_grid_info;
+
+/* Grid::build (src/grid.rs:466-508) then the queries above. */
+dp_status dp_grid_resolve(const dp_grid_spec *spec, dp_grid_info *out);
+
+enum {
+    DP_MAP_TO_CELL = 0,         /* Grid::to_cell, src/grid.rs:695-697 */
+    DP_MAP_TO_POSITION = 1,     /* Grid::to_position, src/grid.rs:700-702 */
+    DP_MAP_CELL_CONTAINING = 2, /* Grid::cell_containing, src/grid.rs:710-714 */
+    DP_MAP_CELL_CENTER = 3      /* Grid::cell_center, src/grid.rs:718-720 (in: integer coords) */
+};
+dp_status dp_grid_map(const dp_grid_spec *spec, uint32_t op, const float in[3], float out[3]);
+
+/* ------------------------------------------------------------------------ */
+/* Resolved scene (host setup): what Simulation::new builds before upload    */
+/* (src/cpu.rs:100-120, src/gpu.rs:190-319).  Host only, needs no GPU.      */
+/* ------------------------------------------------------------------------ */
+
+typedef struct dp_scene dp_scene;
+
+typedef struct dp_scene_info {
+    uint32_t extent[3];
+    uint32_t material_count;
+    float time_step;       /* Grid::time_step, src/grid.rs:592-594 */
+    float courant;
+    float absorber_peak;   /* AbsorbingProfile::peak, src/boundary.rs:215-221 */
+    int32_t reversible;    /* Simulation::is_reversible, src/cpu.rs:209-215 */
+} dp_scene_info;
+
+/* Tables a kernel consumes, readable for parity checks. */
+enum {
+    DP_TABLE_MAGNETIC_GAINS = 0, /* f32 nx+ny+nz: Grid::magnetic_gains, src/grid.rs:602-604 */
+    DP_TABLE_ELECTRIC_GAINS = 1, /* f32 nx+ny+nz: Grid::electric_gains, src/grid.rs:606-608 */
+    DP_TABLE_CELL_CENTERS = 2,   /* f32 nx+ny+nz: Grid::cell_centers, src/grid.rs:649-654 */
+    DP_TABLE_ABSORBER = 3,       /* f32 2*(nx+ny+nz): AbsorbingProfile::packed, src/boundary.rs:203-212 */
+    DP_TABLE_COEFFICIENTS = 4,   /* f32 4*materials: MaterialTable::coefficients, src/material.rs:207-212 */
+    DP_TABLE_MATERIAL_INDEX = 5, /* u8 cells: Scene::material_indices, src/scene.rs:181-206 */
+    DP_TABLE_PRIMARY = 6,        /* f32 nx+ny+nz: Spacing::primary, src/grid.rs:221-223 */
+    DP_TABLE_DUAL = 7            /* f32 nx+ny+nz: Spacing::dual, src/grid.rs:226-228 */
+};
+
+/* Injection (src/source.rs:409-427), flattened for a kernel. */
+typedef struct dp_injection {
+    uint32_t origin[3];
+    uint32_t extent[3];
+    uint32_t component;
+    uint32_t magnetic;
+    float value;                 /* amplitude * waveform(t) */
+    float inverse_waist_squared; /* 0: every cell weighs 1 */
+    float center[3];
+} dp_injection;
+
+/* Replaces the setup half of cpu::Simulation::new / gpu::Simulation::new
+ * (src/cpu.rs:100-120, src/gpu.rs:190-271): grid resolve, coefficient table,
+ * gains, absorber profile, rasterized material index.  Material indices are
+ * stored as u8, so a scene may hold at most 256 materials. */
+dp_status dp_scene_create(const dp_scene_desc *desc, dp_scene **out);
+void dp_scene_destroy(dp_scene *scene);
+dp_status dp_scene_info_get(const dp_scene *scene, dp_scene_info *out);
+/* Copies one table; bytes must equal the table's size exactly. */
+dp_status dp_scene_table(const dp_scene *scene, uint32_t table, void *host, size_t bytes);
+/* Source::injections (src/source.rs:280-403) for every source at `time`,
+ * silenced slots included: 2 per source, in source order. */
+dp_status dp_scene_injections(const dp_scene *scene, float time, dp_injection *out,
+                              uint32_t capacity, uint32_t *count);
+
+/* ------------------------------------------------------------------------ */
+/* Simulation — gpu::Simulation (src/gpu.rs:159-763)                         */
+/* ------------------------------------------------------------------------ */
+
+typedef struct dp_sim dp_sim;
+
+enum {
+    DP_KERNEL_AUTO = 0,  /* fused z-streaming step where the scene allows it */
+    DP_KERNEL_FUSED = 1, /* fused H+E step, TMA plane staging, ping-pong fields */
+    DP_KERNEL_NAIVE = 2  /* one thread per cell, H pass then E pass, in place */
+};
+
+typedef struct dp_options {
+    int32_t device;  /* CUDA ordinal */
+    uint32_t kernel; /* DP_KERNEL_* */
+    uint32_t tile_y; /* fused kernel rows per tile; 0 = tuned default */
+    uint32_t z_chunk;/* fused kernel planes per work unit; 0 = tuned default */
+} dp_options;
+
+enum { DP_FIELD_ELECTRIC = 0, DP_FIELD_MAGNETIC = 1, DP_FIELD_INTENSITY = 2 };
+
+/* gpu::Simulation::new (src/gpu.rs:190-340).  opts may be NULL. */
+dp_status dp_sim_create(const dp_scene *scene, const dp_options *opts, dp_sim **out);
+/* Drop for gpu::Simulation (src/gpu.rs:779-799). */
+void dp_sim_destroy(dp_sim *sim);
+/* advance_by (src/gpu.rs:393-484, src/cpu.rs:200-204): asynchronous. */
+dp_status dp_sim_advance(dp_sim *sim, uint64_t steps);
+/* reverse_by (src/gpu.rs:499-576, src/cpu.rs:275-279): DP_ERR_LOSSY on a
+ * lossy scene, DP_ERR_RANGE past step 0. */
+dp_status dp_sim_reverse(dp_sim *sim, uint64_t steps);
+/* reset (src/gpu.rs:625-637). */
+dp_status dp_sim_reset(dp_sim *sim);
+/* wait (src/gpu.rs:616-622): polls the stream, never traps. */
+dp_status dp_sim_wait(dp_sim *sim, uint32_t timeout_ms);
+/* step_count (src/gpu.rs:357-359). */
+uint64_t dp_sim_step_count(const dp_sim *sim);
+/* time (src/gpu.rs:362-364): step as f32 * dt. */
+float dp_sim_time(const dp_sim *sim);
+/* read_electric / read_magnetic / read_intensity (src/gpu.rs:644-729).
+ * count = 3*cells for E and H, cells for intensity. */
+dp_status dp_sim_read_field(dp_sim *sim, uint32_t field, float *host, size_t count);
+/* Steppable::restore's upload (src/gpu.rs:663-695, 756-762); also seeds an
+ * initial condition like cpu::Simulation::electric_mut (src/cpu.rs:145-151). */
+dp_status dp_sim_write_field(dp_sim *sim, uint32_t field, const float *host, size_t count);
+/* restore (src/gpu.rs:756-762): both fields, the step, intensity cleared. */
+dp_status dp_sim_restore(dp_sim *sim, uint64_t step, const float *electric,
+                         const float *magnetic, size_t count);
+/* set_accumulate_intensity / accumulated_steps (src/gpu.rs:584-594). */
+dp_status dp_sim_set_accumulate_intensity(dp_sim *sim, int on);
+uint64_t dp_sim_accumulated_steps(const dp_sim *sim);
+/* electric_buffer / magnetic_buffer / intensity_buffer (src/gpu.rs:366-374,
+ * 596-599): the live device allocation, valid until the next advance,
+ * reverse or destroy. */
+dp_status dp_sim_device_ptr(dp_sim *sim, uint32_t field, void **ptr);
+/* The simulation's CUDA stream (cudaStream_t), for zero-copy consumers. */
+dp_status dp_sim_stream(dp_sim *sim, void **stream);
+/* bytes_per_step (src/gpu.rs:386-388) = 48 * cells; field_bytes (:377-379). */
+uint64_t dp_sim_bytes_per_step(const dp_sim *sim);
+uint64_t dp_sim_field_bytes(const dp_sim *sim);
+/* energy (src/cpu.rs:654-687), reduced on the device in f64. */
+dp_status dp_sim_energy(dp_sim *sim, double *electric, double *magnetic);
+/* is_finite (src/cpu.rs:707-713), reduced on the device. */
+dp_status dp_sim_is_finite(dp_sim *sim, int32_t *finite);
+/* is_reversible (src/cpu.rs:209-215). */
+int32_t dp_sim_is_reversible(const dp_sim *sim);
+/* Kernel the handle actually runs (DP_KERNEL_FUSED or DP_KERNEL_NAIVE). */
+uint32_t dp_sim_kernel(const dp_sim *sim);
+/* Kernel launches issued by this handle so far (every kernel of this library). */
+uint64_t dp_sim_launch_count(const dp_sim *sim);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIAPHANE_GB300_H */
