@@ -1,0 +1,316 @@
+"""Benchmark: Gcell-updates/s of the fused Yee step on the heterogeneous 512³ scene.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload (both arms): uniform 512³ grid at 1 mm, FP32, 10-cell absorbing
+layer, 200 seeded dielectric spheres (radius 4-24 cells, εr in [1, 4]), a
+perfectly conducting sphere of radius 40 cells, a matched lossy slab, and an
+x-travelling total-field/scattered-field plane wave 16 cells inside the
+absorber (Gaussian pulse, 10 cells per wavelength), intensity accumulation on.
+A step is one full time step (H, sources, E, sources, intensity) of the whole
+grid.  Synthetic data: the scene is generated from a fixed SplitMix64 seed.
+
+ours:       the CUDA library through its C ABI.  `value` is device-timed
+            (CUDA events on the simulation's stream) with the fields resident
+            in HBM; the fields (6.4 GB) dwarf L2, so no flush is needed.
+            `e2e` times the public API end to end with host buffers: restore
+            the fields from pinned host memory, advance K steps, read back
+            the intensity and both fields.
+reference:  the reference's CPU path (its Rust toolchain is absent, so the
+            oracle's C++ restatement of src/cpu.rs), on every host core, on
+            the same scene, for as many steps as fit a bounded time budget.
+
+N > 1 runs independent replicas (the step has no exchange to shard), one
+process per GPU under torchrun; `value` sums all ranks' cells over the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+BYTES_PER_CELL = 48  # 6 f32 components read once and written once (benches/throughput.rs:17-18)
+WORKLOAD = "heterogeneous scatterers 512^3"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=2000)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--side", type=int, default=512, help="grid side (512 is the workload; smaller for checks)")
+    p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-cpu", action="store_true")
+    return p.parse_args()
+
+
+def measured_peaks() -> tuple[float, str]:
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        try:
+            return float(json.loads(path.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(side: int) -> float | None:
+    """DRAM bytes per launch from the committed ncu summary, when one exists."""
+    path = ROOT / "profiles" / "fused_step_heterogeneous.md"
+    if not path.exists():
+        return None
+    for line in path.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch_512:") and side == 512:
+            return float(line.split(":", 1)[1].strip())
+    return None
+
+
+def config(side: int, n: int) -> dict:
+    return {"workload": WORKLOAD if side == 512 else f"heterogeneous scatterers {side}^3",
+            "grid": [side, side, side], "spheres": 200, "materials": 203, "intensity": True,
+            "source": "TFSF plane wave, x-travelling, 26 cells from the low wall",
+            "boundary": "absorbing, 10 cells", "l2": "inputs larger than L2 (fields 6.4 GB), no flush",
+            "parallelism": f"replicas{n}"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.index)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.reader.join(timeout=2)
+
+    def summary(self) -> dict:
+        mhz, maxes, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                mhz.append(float(parts[1]))
+                maxes.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(mhz) if mhz else None, "sm_max_mhz": max(maxes) if maxes else None,
+                "reasons": sorted(reasons), "samples": len(mhz)}
+
+
+def distributed():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_port_rate(scene, threads: int, budget_s: float, max_steps: int, warmup: int) -> tuple[float, int, float]:
+    """Oracle steps on `threads` host cores until the budget is spent."""
+    import oracle
+    sim = oracle.OracleSimulation(scene, threads=threads)
+    sim.set_accumulate_intensity(True)
+    if warmup:
+        sim.advance_by(warmup)
+    steps, start = 0, time.perf_counter()
+    while steps < max_steps:
+        sim.advance_by(1)
+        steps += 1
+        if time.perf_counter() - start > budget_s:
+            break
+    elapsed = time.perf_counter() - start
+    cells = sim.cells
+    return cells * steps / elapsed / 1e9, steps, elapsed
+
+
+def run_reference(args):
+    world, rank, _ = distributed()
+    if rank != 0:
+        return
+    from diaphane_gb300 import workloads
+    threads = os.cpu_count() or 1
+    scene = workloads.heterogeneous(args.side)
+    rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=60.0, max_steps=args.steps,
+                                         warmup=min(args.warmup, 1))
+    sample = (f"{steps} oracle steps of the full {args.side}^3 scene in {elapsed:.1f} s "
+              f"(time-budgeted; the per-step cost is constant)")
+    line = {"impl": "reference", "metric": "Gcell-updates/s", "value": rate, "unit": "Gcell/s", "n_gpus": world,
+            "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * elapsed / max(steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded SplitMix64 scene)", "config": config(args.side, world),
+            "cpu_baseline": {"value": rate, "unit": "Gcell/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference is Rust (cargo absent on both machines); this is the oracle's C++ restatement "
+                    "of src/cpu.rs with OpenMP over z planes"}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    world, rank, local = distributed()
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", init_method="env://")
+    device = local if world > 1 else 0
+
+    from diaphane_gb300 import DP_KERNEL_AUTO, ResolvedScene, Simulation, workloads
+    from diaphane_gb300.build import build
+    build()
+
+    scene = workloads.heterogeneous(args.side)
+    resolved = ResolvedScene(scene)
+    sim = Simulation(resolved, kernel=DP_KERNEL_AUTO, device=device)
+    sim.set_accumulate_intensity(True)
+    stream = torch.cuda.ExternalStream(sim_stream(sim), device=device)
+    cells = sim.cells
+
+    def barrier():
+        torch.cuda.synchronize(device)
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    sim.advance_by(args.warmup)
+    sim.wait()
+    barrier()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = sim.launch_count()
+    with ClockSampler(device) as clocks:
+        start.record(stream)
+        sim.advance_by(args.steps)
+        end.record(stream)
+        sim.wait(600_000)
+        barrier()
+    launches = sim.launch_count() - launches0
+    ms = start.elapsed_time(end)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    seconds = ms / 1e3
+    value = world * cells * args.steps / seconds / 1e9
+
+    # End to end through the public API, host buffers, copies inside the clock.
+    e2e = None
+    if not args.no_e2e:
+        pinned_e = torch.empty(3 * cells, dtype=torch.float32, pin_memory=True)
+        pinned_h = torch.empty(3 * cells, dtype=torch.float32, pin_memory=True)
+        pinned_i = torch.empty(cells, dtype=torch.float32, pin_memory=True)
+        pinned_e.zero_()
+        pinned_h.zero_()
+        from diaphane_gb300 import Snapshot
+        barrier()
+        t0 = time.perf_counter()
+        sim.restore(Snapshot(0, pinned_e.numpy(), pinned_h.numpy()))
+        sim.set_accumulate_intensity(False)
+        sim.set_accumulate_intensity(True)
+        sim.advance_by(args.steps)
+        read_into(sim, pinned_i, pinned_e, pinned_h)
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([e2e_s], device=f"cuda:{device}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        h2d = 24 * cells / args.steps
+        d2h = 28 * cells / args.steps
+        e2e = {"value": world * cells * args.steps / e2e_s / 1e9, "unit": "Gcell/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+               "what": "restore E,H from pinned host memory; advance K steps with intensity; "
+                       "read intensity, E and H back; wall clock"}
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peaks()
+    achieved = BYTES_PER_CELL * cells / (seconds / args.steps) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profiled_traffic(args.side), "peak_kind": peak_kind,
+                "algorithmic_bytes_per_launch": BYTES_PER_CELL * cells,
+                "note": "48 B/cell-update of field traffic; the u8 material index (1 B) and the "
+                        "intensity read-modify-write (8 B) move on top of it"}
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=12.0, max_steps=200, warmup=0)
+        cpu = {"value": rate, "unit": "Gcell/s", "cores": threads, "kind": "port",
+               "sample": f"{steps} oracle steps of the same {args.side}^3 scene, {elapsed:.1f} s"}
+    line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64 scene)",
+            "config": config(args.side, world), "kernel": ["", "fused", "naive"][sim.kernel],
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def sim_stream(sim) -> int:
+    import ctypes as C
+    from diaphane_gb300 import _abi
+    p = C.c_void_p()
+    _abi.check(_abi.lib().dp_sim_stream(sim.handle, C.byref(p)))
+    return p.value or 0
+
+
+def read_into(sim, intensity, electric, magnetic) -> None:
+    from diaphane_gb300 import _abi
+    lib = _abi.lib()
+    _abi.check(lib.dp_sim_read_field(sim.handle, _abi.DP_FIELD_INTENSITY, intensity.data_ptr(), intensity.numel()))
+    _abi.check(lib.dp_sim_read_field(sim.handle, _abi.DP_FIELD_ELECTRIC, electric.data_ptr(), electric.numel()))
+    _abi.check(lib.dp_sim_read_field(sim.handle, _abi.DP_FIELD_MAGNETIC, magnetic.data_ptr(), magnetic.numel()))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

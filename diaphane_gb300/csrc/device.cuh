@@ -59,18 +59,29 @@ void launch_energy(const DeviceScene &s, FieldSet f, const float *primary, const
 void launch_finite(const DeviceScene &s, FieldSet f, int32_t *flag, cudaStream_t stream);
 uint32_t energy_blocks(uint64_t cells);
 
-// Fused path (kernels_fused.cu): one launch per step, reads `in`, writes `out`.
+// Fused path (kernels_fused.cu): one launch per step, reads one field set
+// (through TMA tensor maps) and writes the other.
 struct FusedPlan {
     uint32_t tile_y;   // rows per tile
-    uint32_t z_chunk;  // planes per work unit
+    uint32_t cx;       // cells per lane along x (tile width 32*cx)
+    uint32_t z_chunk;  // planes per CTA
     uint32_t tiles_x, tiles_y, chunks;
     uint32_t grid;     // CTAs launched
     size_t smem;       // dynamic shared memory per CTA
 };
+// Opaque 128-byte CUtensorMap images for one input field set.
+struct FusedMaps {
+    alignas(64) unsigned char e[128];
+    alignas(64) unsigned char h[128];
+    alignas(64) unsigned char m[128];
+};
 bool fused_supported(const uint32_t n[3]);
 FusedPlan fused_plan(const uint32_t n[3], uint32_t tile_y, uint32_t z_chunk, int sm_count);
-void launch_fused_step(const DeviceScene &s, const FusedPlan &plan, FieldSet in, FieldSet out,
-                       float *intensity, const InjectionTable &table, uint32_t *work_counter,
-                       cudaStream_t stream);
+// material_padded: the u8 index with rows padded to material_pitch (a
+// multiple of 16) so the tensor map's row stride is 16-byte aligned.
+void fused_maps(const DeviceScene &s, const FusedPlan &plan, FieldSet set, const uint8_t *material_padded,
+                uint32_t material_pitch, FusedMaps &out);
+void launch_fused_step(const DeviceScene &s, const FusedPlan &plan, const FusedMaps &in_maps, FieldSet out,
+                       float *intensity, const InjectionTable &table, int32_t *error, cudaStream_t stream);
 
 } // namespace diaphane

@@ -60,8 +60,11 @@ struct dp_sim {
     double *partials = nullptr;
     double *host_partials = nullptr;
     int32_t *flag = nullptr;
-    uint32_t *work_counter = nullptr;
+    int32_t *error = nullptr;        // set by a kernel whose bounded wait gave up
+    uint8_t *material_padded = nullptr;
+    uint32_t material_pitch = 0;
     FusedPlan plan{};
+    FusedMaps maps[2]{};             // tensor maps reading set 0 / set 1
     std::vector<void *> owned;
     uint64_t step = 0;
     uint64_t accumulated = 0;
@@ -123,8 +126,8 @@ struct dp_sim {
                 InjectionTable table{};
                 table.count = uint32_t(all.size());
                 for (size_t k = 0; k < all.size(); ++k) table.item[k] = all[k];
-                launch_fused_step(dev, plan, set[current], set[current ^ 1], accumulating ? intensity : nullptr,
-                                  table, work_counter, stream);
+                launch_fused_step(dev, plan, maps[current], set[current ^ 1], accumulating ? intensity : nullptr,
+                                  table, error, stream);
                 ++launches;
                 current ^= 1;
             } else {
@@ -173,10 +176,18 @@ struct dp_sim {
         const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
         for (;;) {
             cudaError_t q = cudaStreamQuery(stream);
-            if (q == cudaSuccess) return;
+            if (q == cudaSuccess) break;
             if (q != cudaErrorNotReady) check(q, "stream");
             if (std::chrono::steady_clock::now() >= deadline) throw Error(DP_ERR_TIMEOUT, "the GPU did not finish in time");
             std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+        if (kernel == DP_KERNEL_FUSED) {
+            int32_t code = 0;
+            check(cudaMemcpy(&code, error, sizeof(code), cudaMemcpyDeviceToHost), "error flag");
+            if (code != 0) {
+                check(cudaMemset(error, 0, sizeof(int32_t)), "error flag");
+                throw Error(DP_ERR_TIMEOUT, "a fused step gave up waiting for its plane loads");
+            }
         }
     }
 };
@@ -211,9 +222,12 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
     for (int a = 0; a < 3; ++a) d.n[a] = s.grid.n[a];
     d.cells = cells;
     d.material = device_upload(s.material_index, owned, st);
-    std::vector<float4> coeff;
-    for (const Coeff &c : s.coefficients)
-        coeff.push_back(make_float4(c.electric_gain, c.electric_loss, c.magnetic_gain, c.magnetic_loss));
+    // Padded to all 256 u8 indices, so a kernel may stage the whole table.
+    std::vector<float4> coeff(256, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    for (size_t m = 0; m < s.coefficients.size(); ++m) {
+        const Coeff &c = s.coefficients[m];
+        coeff[m] = make_float4(c.electric_gain, c.electric_loss, c.magnetic_gain, c.magnetic_loss);
+    }
     d.coeff = device_upload(coeff, owned, st);
     d.mgain = device_upload(s.magnetic_gains, owned, st);
     d.egain = device_upload(s.electric_gains, owned, st);
@@ -239,13 +253,27 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
     sim->partials = device_alloc<double>(2 * size_t(blocks), owned);
     check(cudaMallocHost(&sim->host_partials, 2 * size_t(blocks) * sizeof(double)), "cudaMallocHost");
     sim->flag = device_alloc<int32_t>(1, owned);
-    sim->work_counter = device_alloc<uint32_t>(2, owned);
-    check(cudaMemsetAsync(sim->work_counter, 0, 2 * sizeof(uint32_t), st), "memset");
+    sim->error = device_alloc<int32_t>(1, owned);
+    check(cudaMemsetAsync(sim->error, 0, sizeof(int32_t), st), "memset");
 
     if (sim->kernel == DP_KERNEL_FUSED) {
         int sms = 0;
         check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sim->device), "attribute");
         sim->plan = fused_plan(s.grid.n, opts ? opts->tile_y : 0, opts ? opts->z_chunk : 0, sms);
+        // The index again with rows padded to 16 bytes, for its tensor map.
+        const uint32_t nx = s.grid.n[0], rows = s.grid.n[1] * s.grid.n[2];
+        sim->material_pitch = (nx + 15) / 16 * 16;
+        std::vector<uint8_t> padded(size_t(sim->material_pitch) * rows, 0);
+        for (size_t r = 0; r < rows; ++r)
+            std::memcpy(&padded[r * sim->material_pitch], &s.material_index[r * nx], nx);
+        sim->material_padded = device_upload(padded, owned, st);
+        check(cudaStreamSynchronize(st), "setup upload");
+        try {
+            for (int k = 0; k < 2; ++k)
+                fused_maps(d, sim->plan, sim->set[k], sim->material_padded, sim->material_pitch, sim->maps[k]);
+        } catch (const std::exception &e) {
+            throw Error(DP_ERR_CUDA, e.what());
+        }
     }
     check(cudaStreamSynchronize(st), "setup upload");
     return sim.release();

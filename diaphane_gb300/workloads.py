@@ -1,0 +1,127 @@
+"""Seeded synthetic scenes for the benchmark workloads.
+
+There is no public dataset behind these: each is a scene generated from a
+seed with the sizes and value ranges the workload names, using SplitMix64 so
+the same seed gives the same scene on any machine.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from .scene import Axis, Boundary, Extent, Grid, Material, Refinement, Scene, Shape, Source, Waveform, f32
+
+MASK = (1 << 64) - 1
+
+
+class SplitMix64:
+    """Steele, Lea and Flood's SplitMix64 generator."""
+
+    def __init__(self, seed: int):
+        self.state = seed & MASK
+
+    def next_u64(self) -> int:
+        self.state = (self.state + 0x9E3779B97F4A7C15) & MASK
+        z = self.state
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & MASK
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & MASK
+        return z ^ (z >> 31)
+
+    def uniform(self, lo: float, hi: float) -> float:
+        return lo + (hi - lo) * ((self.next_u64() >> 11) * (1.0 / (1 << 53)))
+
+
+HETEROGENEOUS_SEED = 0x5EED_0002
+
+
+def heterogeneous(side: int = 512, spheres: int = 200, seed: int = HETEROGENEOUS_SEED) -> Scene:
+    """Heterogeneous scatterers on a uniform side³ grid at 1 mm.
+
+    * 10-cell absorbing layer (R0 = 1e-6).
+    * `spheres` dielectric spheres, radius uniform in [4, 24] cells, εr
+      uniform in [1, 4], centres uniform over the interior but kept two cells
+      clear of the absorber and of the plane-wave correction rows (which must
+      be vacuum, src/source.rs:177-180).  Each sphere is its own material.
+    * One perfectly conducting sphere of radius 40 cells at the centre.
+    * One lossy slab, Material::matched_lossy(2, σ), 16 cells thick across x
+      at 3/4 of the domain, with σ chosen so the electric half-step loss
+      σ·Δt/(2ε0εr) is 0.02; matched magnetic loss keeps it reflectionless.
+    * An x-travelling, z-polarized plane wave (total-field/scattered-field,
+      src/source.rs:334-401) entering 16 cells inside the absorber, i.e. 26
+      cells from the low x wall; Gaussian pulse, 3 cycles, at the frequency
+      whose wavelength is 10 cells.
+    Painted in that order: spheres, then the conductor, then the slab.
+    """
+    rng = SplitMix64(seed)
+    cell = f32(1e-3)
+    scene = Scene.empty(Extent.cube(side), float(cell))
+    grid = scene.grid
+    half = side * float(cell) / 2.0
+    absorber, inset = 10, 16
+    plane_cell = absorber + inset
+
+    def position(c: float) -> float:
+        return float(f32(c) * cell - f32(half))
+
+    for _ in range(spheres):
+        r = rng.uniform(4.0, 24.0)
+        eps = rng.uniform(1.0, 4.0)
+        lo_x, hi_x = plane_cell + 2 + r, side - absorber - 2 - r
+        lo, hi = absorber + 2 + r, side - absorber - 2 - r
+        cx, cy, cz = rng.uniform(lo_x, hi_x), rng.uniform(lo, hi), rng.uniform(lo, hi)
+        m = scene.materials.push(Material.dielectric(eps))
+        scene.shapes.append(Shape.sphere((position(cx), position(cy), position(cz)), float(f32(r) * cell), m))
+
+    pec = scene.materials.push(Material.PERFECT_CONDUCTOR)
+    scene.shapes.append(Shape.sphere((0.0, 0.0, 0.0), float(f32(40.0) * cell), pec))
+
+    dt = grid.time_step()
+    eps_slab = 2.0
+    sigma = 0.02 * 2.0 * 8.854188e-12 * eps_slab / dt
+    lossy = scene.materials.push(Material.matched_lossy(eps_slab, sigma))
+    scene.shapes.append(Shape.slab(Axis.X, position(0.75 * side), float(f32(16.0) * cell), lossy))
+
+    frequency = grid.frequency_for_resolution(10.0)
+    scene.sources.append(Source.plane_wave(Axis.X, position(plane_cell + 0.5), Axis.Z,
+                                           Waveform.gaussian_pulse(frequency, 3.0)))
+    return scene
+
+
+def free_flight(side: int = 80) -> Scene:
+    """Uniform side³ at 1 mm, vacuum, Courant 0.99/√3, 10-cell absorber, Ez
+    point source at the centre: Gaussian-modulated sinusoid at 30 GHz with
+    50% bandwidth, read as an amplitude-spectrum FWHM of 15 GHz, which is a
+    time-envelope FWHM of 4·ln2/(π·15 GHz) = 58.8 ps = 1.765 carrier cycles."""
+    scene = Scene.empty(Extent.cube(side), 1e-3)
+    scene.grid.courant = float(f32(0.99) / f32(math.sqrt(3.0)))
+    cycles = 4.0 * math.log(2.0) / (math.pi * 15e9) * 30e9
+    scene.sources.append(Source.point((0.0, 0.0, 0.0), Axis.Z, Waveform.gaussian_pulse(30e9, cycles)))
+    return scene
+
+
+def graded_stack(open_boundary: bool = True) -> Scene:
+    """640×256×256 graded layered stack: x graded at cap 1.15 from 1 mm down
+    to 0.1 mm across an 8 mm band, y and z uniform at 1 mm; six quarter-wave
+    pairs of n = 1.5 and n = 2.3 fill the band (λ0 = 4·8 mm/(6·(1/1.5... see
+    below)); a sheet source at λ0 in vacuum launches into it."""
+    grid = Grid.graded((0.549, 0.256, 0.256), 1000.0, [Refinement.across(Axis.X, 0.0, 0.008, 1e-4)], 1.15)
+    scene = Scene.on_grid(grid)
+    if not open_boundary:
+        scene.boundary = Boundary.PEC
+    # Quarter-wave pair: d1 = λ0/(4·1.5), d2 = λ0/(4·2.3); six pairs fill
+    # 8 mm, so λ0 = 8 mm·4/(6·(1/1.5 + 1/2.3)) = 4.84 mm (f0 = 61.9 GHz).
+    n1, n2 = 1.5, 2.3
+    lam0 = 0.008 * 4.0 / (6.0 * (1.0 / n1 + 1.0 / n2))
+    d1, d2 = lam0 / (4 * n1), lam0 / (4 * n2)
+    m1 = scene.materials.push(Material.refractive(n1))
+    m2 = scene.materials.push(Material.refractive(n2))
+    x = -0.004
+    for _ in range(6):
+        scene.shapes.append(Shape.slab(Axis.X, x + d1 / 2, d1, m1))
+        x += d1
+        scene.shapes.append(Shape.slab(Axis.X, x + d2 / 2, d2, m2))
+        x += d2
+    f0 = 299792458.0 / lam0
+    scene.sources.append(Source.sheet(Axis.X, -0.15, 0.06, Axis.Z, Waveform.gaussian_pulse(f0, 3.0)))
+    return scene
