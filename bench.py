@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--side", type=int, default=512, help="grid side (512 is the workload; smaller for checks)")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--variant", default="", help="fused kernel cx,tile_y,slots (default: tuned)")
     p.add_argument("--no-cpu", action="store_true")
     return p.parse_args()
 
@@ -202,7 +203,9 @@ def run_ours(args):
 
     scene = workloads.heterogeneous(args.side)
     resolved = ResolvedScene(scene)
-    sim = Simulation(resolved, kernel=DP_KERNEL_AUTO, device=device)
+    v = [int(t) for t in args.variant.split(",")] if args.variant else [0, 0, 0]
+    sim = Simulation(resolved, kernel=DP_KERNEL_AUTO, device=device, cells_per_lane=v[0], tile_y=v[1],
+                     ring_slots=v[2])
     sim.set_accumulate_intensity(True)
     stream = torch.cuda.ExternalStream(sim_stream(sim), device=device)
     cells = sim.cells
@@ -283,6 +286,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64 scene)",
             "config": config(args.side, world), "kernel": ["", "fused", "naive"][sim.kernel],
+            "variant": args.variant or "default",
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)

@@ -85,7 +85,8 @@ class dp_injection(C.Structure):
 
 
 class dp_options(C.Structure):
-    _fields_ = [("device", C.c_int32), ("kernel", C.c_uint32), ("tile_y", C.c_uint32), ("z_chunk", C.c_uint32)]
+    _fields_ = [("device", C.c_int32), ("kernel", C.c_uint32), ("tile_y", C.c_uint32), ("z_chunk", C.c_uint32),
+                ("cells_per_lane", C.c_uint32), ("ring_slots", C.c_uint32)]
 
 
 # Every entry point declared in include/diaphane_gb300.h: (name, restype, argtypes).

@@ -62,12 +62,14 @@ uint32_t energy_blocks(uint64_t cells);
 // Fused path (kernels_fused.cu): one launch per step, reads one field set
 // (through TMA tensor maps) and writes the other.
 struct FusedPlan {
-    uint32_t tile_y;   // rows per tile
-    uint32_t cx;       // cells per lane along x (tile width 32*cx)
-    uint32_t z_chunk;  // planes per CTA
+    uint32_t tile_y;      // rows per tile, one warp each
+    uint32_t cx;          // cells per lane along x (tile width 32*cx)
+    uint32_t slots;       // z-planes in the shared-memory ring
+    uint32_t ctas_per_sm; // resident CTAs per SM the variant is sized for
+    uint32_t z_chunk;     // planes per CTA
     uint32_t tiles_x, tiles_y, chunks;
-    uint32_t grid;     // CTAs launched
-    size_t smem;       // dynamic shared memory per CTA
+    uint32_t grid;        // CTAs launched
+    size_t smem;          // dynamic shared memory per CTA
 };
 // Opaque 128-byte CUtensorMap images for one input field set.
 struct FusedMaps {
@@ -76,7 +78,10 @@ struct FusedMaps {
     alignas(64) unsigned char m[128];
 };
 bool fused_supported(const uint32_t n[3]);
-FusedPlan fused_plan(const uint32_t n[3], uint32_t tile_y, uint32_t z_chunk, int sm_count);
+bool fused_variant_exists(uint32_t cx, uint32_t tile_y, uint32_t slots);
+// Zero for cx, tile_y, slots or z_chunk picks the default.
+FusedPlan fused_plan(const uint32_t n[3], uint32_t cx, uint32_t tile_y, uint32_t slots, uint32_t z_chunk,
+                     int sm_count);
 // material_padded: the u8 index with rows padded to material_pitch (a
 // multiple of 16) so the tensor map's row stride is 16-byte aligned.
 void fused_maps(const DeviceScene &s, const FusedPlan &plan, FieldSet set, const uint8_t *material_padded,

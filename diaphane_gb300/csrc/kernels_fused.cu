@@ -10,8 +10,9 @@
 //     CTA still needs (the reference updates in place because its two passes
 //     are separated by a barrier; a fused pass cannot be);
 //   * halo recompute: E at the tile's low x column and low y row needs new H
-//     one cell outside the tile, so a ninth warp recomputes H there from the
-//     same inputs instead of waiting for the neighbouring CTA.
+//     one cell outside the tile, so the CTA recomputes H there from the same
+//     inputs instead of waiting for the neighbouring CTA (each warp takes an
+//     eighth of the halo row and the halo cell of its own row).
 // Each cell's six components are then read once and written once per step:
 // the 48 B/cell of the reference's own accounting (src/gpu.rs:381-388).
 //
@@ -43,19 +44,21 @@ namespace diaphane {
 
 namespace {
 
-constexpr int kTileY = 8;                 // rows per tile, one compute warp each
-constexpr int kWarps = kTileY + 1;        // + the halo warp
-constexpr int kThreads = kWarps * 32;
-constexpr int kSlots = 3;                 // plane ring depth
 constexpr int kMaxMaterials = 256;
 constexpr long long kWaitCycles = 1ll << 32; // ~2 s at 2 GHz, then give up
 
-template <int CX> struct Geometry {
+// CX cells per lane along x, TY rows per tile (one warp each), SLOTS planes
+// in the shared-memory ring.
+template <int CX, int TY, int SLOTS> struct Geometry {
+    static constexpr int kTileY = TY;
+    static constexpr int kWarps = TY;
+    static constexpr int kThreads = 32 * TY;
+    static constexpr int kSlots = SLOTS;
     static constexpr int TX = 32 * CX;         // tile width in cells
     static constexpr int W = TX + 8;           // E/H row: 4 cells of halo each side (TMA wants 16 B)
     static constexpr int WM = TX + 32;         // index row: 16 cells each side
-    static constexpr int ER = kTileY + 2;      // E rows: y0-1 .. y0+TY
-    static constexpr int HR = kTileY + 1;      // H rows: y0-1 .. y0+TY-1
+    static constexpr int ER = TY + 2;          // E rows: y0-1 .. y0+TY
+    static constexpr int HR = TY + 1;          // H rows: y0-1 .. y0+TY-1
     static constexpr int E_BYTES = 3 * ER * W * 4;
     static constexpr int H_BYTES = 3 * HR * W * 4;
     static constexpr int M_BYTES = HR * WM;
@@ -188,54 +191,102 @@ __device__ __forceinline__ float ldg_at(const float *base, int i, int n) {
     return (i >= 0 && i < n) ? __ldg(base + i) : 0.0f;
 }
 
-// The reference's semi-implicit updates (src/material.rs:131-146).  A zero
-// total loss reduces ((1-l)v ± g·c)/(1+l) to v ± g·c exactly.
-__device__ __forceinline__ float h_update(float h, float loss, float gain, float curl) {
-    if (loss == 0.0f) return h - gain * curl;
+// The reference's semi-implicit updates (src/material.rs:131-146), in full.
+// With a total loss of exactly zero they reduce to v ∓ g·c bit for bit, which
+// is what the fast path below computes; either form is exact for l = 0.
+__device__ __forceinline__ float h_full(float h, float loss, float gain, float curl) {
     return ((1.0f - loss) * h - gain * curl) / (1.0f + loss);
 }
 
-__device__ __forceinline__ float e_update(float e, float loss, float gain, float curl) {
-    if (loss == 0.0f) return e + gain * curl;
+__device__ __forceinline__ float e_full(float e, float loss, float gain, float curl) {
     return ((1.0f - loss) * e + gain * curl) / (1.0f + loss);
 }
 
-// Adds every injection of one phase that targets (component, cell) in the
-// order the host listed them, which is the reference's order.
-__device__ __forceinline__ float inject(const InjectionTable &t, const DeviceScene &s, bool magnetic,
-                                        uint32_t component, int x, int y, int z, float value) {
+// Bit k is set when injection k of `magnetic` phase covers row y and any of
+// the cells [xa, xb).  Computed once per thread; the per-plane test is then a
+// single z comparison per set bit.
+__device__ __forceinline__ uint32_t injection_mask(const InjectionTable &t, bool magnetic, int xa, int xb, int y) {
+    uint32_t m = 0;
     for (uint32_t k = 0; k < t.count; ++k) {
         const DeviceInjection &d = t.item[k];
-        if (d.magnetic != uint32_t(magnetic) || d.component != component) continue;
-        const int dx = x - int(d.origin[0]), dy = y - int(d.origin[1]), dz = z - int(d.origin[2]);
-        if (dx < 0 || dy < 0 || dz < 0 || dx >= int(d.extent[0]) || dy >= int(d.extent[1]) || dz >= int(d.extent[2]))
-            continue;
-        const float weight = d.weight_offset < 0
-                                 ? 1.0f
-                                 : __ldg(&s.weights[d.weight_offset + (uint64_t(dz) * d.extent[1] + dy) * d.extent[0] + dx]);
-        value += d.value * weight;
+        if (d.magnetic == uint32_t(magnetic) && y >= int(d.origin[1]) && y < int(d.origin[1] + d.extent[1]) &&
+            xb > int(d.origin[0]) && xa < int(d.origin[0] + d.extent[0]))
+            m |= 1u << k;
     }
-    return value;
+    return m;
 }
 
-// Does any injection of this phase touch plane z / row y at all?
-__device__ __forceinline__ bool touches(const InjectionTable &t, bool magnetic, int y, int z) {
-    for (uint32_t k = 0; k < t.count; ++k) {
-        const DeviceInjection &d = t.item[k];
-        if (d.magnetic == uint32_t(magnetic) && z >= int(d.origin[2]) && z < int(d.origin[2] + d.extent[2]) &&
-            y >= int(d.origin[1]) && y < int(d.origin[1] + d.extent[1]))
-            return true;
-    }
-    return false;
-}
-
+// Adds the injections in `mask` to the CX cells starting at x, in table
+// order — the reference's order (src/cpu.rs:606-633).
 template <int CX>
-__global__ void __launch_bounds__(kThreads, 2)
+__device__ __forceinline__ void apply_injections(const InjectionTable &t, const float *weights, uint32_t mask, int x,
+                                                 int y, int z, Vec<CX> &f0, Vec<CX> &f1, Vec<CX> &f2) {
+    while (mask) {
+        const int k = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const DeviceInjection &d = t.item[k];
+        const int dz = z - int(d.origin[2]);
+        if (dz < 0 || dz >= int(d.extent[2])) continue;
+        const int dy = y - int(d.origin[1]);
+#pragma unroll
+        for (int j = 0; j < CX; ++j) {
+            const int dx = x + j - int(d.origin[0]);
+            if (dx < 0 || dx >= int(d.extent[0])) continue;
+            const float w = d.weight_offset < 0
+                                ? 1.0f
+                                : __ldg(&weights[d.weight_offset + (uint64_t(dz) * d.extent[1] + dy) * d.extent[0] + dx]);
+            const float add = d.value * w;
+            if (d.component == 0) f0.v[j] += add;
+            else if (d.component == 1) f1.v[j] += add;
+            else f2.v[j] += add;
+        }
+    }
+}
+
+__device__ __forceinline__ void apply_injections_1(const InjectionTable &t, const float *weights, uint32_t mask,
+                                                   int x, int y, int z, float &f0, float &f1, float &f2) {
+    Vec<1> a{{f0}}, b{{f1}}, c{{f2}};
+    apply_injections<1>(t, weights, mask, x, y, z, a, b, c);
+    f0 = a.v[0];
+    f1 = b.v[0];
+    f2 = c.v[0];
+}
+
+// CX material indices of one lane, from its slot row.
+template <int CX> __device__ __forceinline__ void load_materials(const uint8_t *p, uint32_t out[CX]) {
+    if constexpr (CX == 4) {
+        const uint32_t w = *reinterpret_cast<const uint32_t *>(p);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) out[j] = (w >> (8 * j)) & 0xffu;
+    } else if constexpr (CX == 2) {
+        const uint32_t w = *reinterpret_cast<const uint16_t *>(p);
+        out[0] = w & 0xffu;
+        out[1] = w >> 8;
+    } else {
+        out[0] = *p;
+    }
+}
+
+// One H cell update of all three components from slot values: used for the
+// halo cells, where each lane owns a single cell.
+struct HaloCell {
+    int hr, hc;                  // slot row and column
+    float mgx, mgy, aix, ahx, aiy, ahy;
+    uint32_t mask;               // magnetic injections covering the cell
+    int x, y;
+};
+
+// Sixteen resident warps x 128 registers fill each SM sub-partition's
+// 16K-register file exactly: two CTAs of 8 warps, or one of 16.
+template <int CX, int TY, int SLOTS>
+__global__ void __launch_bounds__(32 * TY, 16 / TY)
 fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CUtensorMap h_map,
            const __grid_constant__ CUtensorMap m_map, const __grid_constant__ FusedArgs args) {
-    using G = Geometry<CX>;
+    using G = Geometry<CX, TY, SLOTS>;
+    constexpr int kTileY = G::kTileY, kWarps = G::kWarps, kThreads = G::kThreads, kSlots = G::kSlots;
     extern __shared__ __align__(128) unsigned char smem[];
     const DeviceScene &s = args.s;
+    const InjectionTable &inj = args.inj;
     const int nx = int(s.n[0]), ny = int(s.n[1]), nz = int(s.n[2]);
     const uint64_t cells = s.cells;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -276,9 +327,8 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
         for (int p = zs; p <= min(zs + kSlots - 1, last_plane); ++p) issue(p);
 
     // Per-thread constants: this lane's cells along x, this warp's row.
-    const bool halo = warp == kTileY;
-    const int row = halo ? 0 : warp + 1;     // row in the H slot (and E slot)
-    const int y = y0 + row - 1;
+    const int row = warp + 1;                // row in the E and H slots
+    const int y = y0 + warp;
     const int xl = x0 + CX * lane;           // first cell of this lane
     const int col = 4 + CX * lane;           // its column in an E/H slot row
     const int mcol = 16 + CX * lane;         // its column in an index slot row
@@ -289,13 +339,37 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
     const Vec<CX> aix = ldg_x<CX>(absorb_int, xl, nx), ahx = ldg_x<CX>(absorb_half, xl, nx);
     const float mgy = ldg_at(s.mgain + nx, y, ny), egy = ldg_at(s.egain + nx, y, ny);
     const float aiy = ldg_at(absorb_int + nx, y, ny), ahy = ldg_at(absorb_half + nx, y, ny);
-    // The halo column (x0-1) is handled by halo-warp lanes 0..TY-1, one row each.
-    const int hy_row = lane + 1, hy_y = y0 + lane;
-    const float hc_mgx = ldg_at(s.mgain, x0 - 1, nx);
-    const float hc_ahx = ldg_at(absorb_half, x0 - 1, nx);
-    const float hc_mgy = ldg_at(s.mgain + nx, hy_y, ny);
-    const float hc_aiy = ldg_at(absorb_int + nx, hy_y, ny), hc_ahy = ldg_at(absorb_half + nx, hy_y, ny);
-    const bool store_row = !halo && y < ny && xl < nx;
+    const bool store_row = y < ny && xl < nx;
+    const bool has_inj = inj.count != 0;
+    const uint32_t mask_h = has_inj ? injection_mask(inj, true, xl, xl + CX, y) : 0u;
+    const uint32_t mask_e = has_inj ? injection_mask(inj, false, xl, xl + CX, y) : 0u;
+
+    // Halo cells: lanes 0..4CX-1 of warp w take cells [4CX·w, 4CX·(w+1)) of
+    // row y0-1 (the Hx, Hz that E at row y0 reads); lane 4CX takes the cell
+    // (x0-1, y) of the warp's own row (the Hy, Hz that E at x0 reads).
+    constexpr int kHaloRowLanes = G::TX / kWarps;
+    const bool halo_lane = lane <= kHaloRowLanes;
+    HaloCell hc{};
+    if (halo_lane) {
+        if (lane < kHaloRowLanes) {
+            hc.hr = 0;
+            hc.hc = 4 + kHaloRowLanes * warp + lane;
+            hc.x = x0 + kHaloRowLanes * warp + lane;
+            hc.y = y0 - 1;
+        } else {
+            hc.hr = row;
+            hc.hc = 3;
+            hc.x = x0 - 1;
+            hc.y = y;
+        }
+        hc.mgx = ldg_at(s.mgain, hc.x, nx);
+        hc.aix = ldg_at(absorb_int, hc.x, nx);
+        hc.ahx = ldg_at(absorb_half, hc.x, nx);
+        hc.mgy = ldg_at(s.mgain + nx, hc.y, ny);
+        hc.aiy = ldg_at(absorb_int + nx, hc.y, ny);
+        hc.ahy = ldg_at(absorb_half + nx, hc.y, ny);
+        hc.mask = has_inj ? injection_mask(inj, true, hc.x, hc.x + 1, hc.y) : 0u;
+    }
 
     Vec<CX> hx_prev, hy_prev; // new H at plane z-1, this thread's cells
 #pragma unroll
@@ -304,9 +378,13 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
     for (int p = zs; p < z1; ++p) {
         const int k = (p - zs) % kSlots, k1 = (p + 1 - zs) % kSlots;
         const uint32_t phase = uint32_t((p - zs) / kSlots) & 1u, phase1 = uint32_t((p + 1 - zs) / kSlots) & 1u;
+        // One thread polls the ring; the others park in the hardware barrier
+        // below instead of spending issue slots on the poll.
         bool ok = true;
-        if (p == zs) ok = mbar_wait_bounded(bar0 + 8 * k, phase, kWaitCycles);
-        ok = ok && mbar_wait_bounded(bar0 + 8 * k1, phase1, kWaitCycles);
+        if (threadIdx.x == 0) {
+            if (p == zs) ok = mbar_wait_bounded(bar0 + 8 * k, phase, kWaitCycles);
+            ok = ok && mbar_wait_bounded(bar0 + 8 * k1, phase1, kWaitCycles);
+        }
         if (__syncthreads_or(!ok)) {
             // Give up on this chunk: report, then let the loads already in
             // flight land before the CTA's shared memory goes away.
@@ -336,15 +414,18 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
         const bool prologue = p < z0;
         const float mgz = __ldg(&s.mgain[nx + ny + p]), egz = __ldg(&s.egain[nx + ny + p]);
         const float aiz = __ldg(&absorb_int[nx + ny + p]), ahz = __ldg(&absorb_half[nx + ny + p]);
-        const uint64_t plane_base = uint64_t(p) * ny * nx;
+        const uint64_t at = uint64_t(p) * ny * nx + uint64_t(y) * nx + xl; // this lane's first cell
 
         // Intensity of this thread's cells, fetched early.
         Vec<CX> inten;
         const bool accumulate = args.intensity != nullptr && !prologue && store_row;
-        if (accumulate) inten = ldg<CX>(args.intensity + plane_base + uint64_t(y) * nx + xl);
+        if (accumulate) inten = ldg<CX>(args.intensity + at);
 
-        // ---------------- H(p) ----------------
-        if (!halo) {
+        // Material coefficients of this lane's cells, kept for the E phase.
+        float2 ecoef[CX]; // (electric_gain, electric_loss)
+
+        // ---------------- H(p): this warp's row ----------------
+        {
             const Vec<CX> ex = lds<CX>(e_at(E, 0, row, col)), ex_up = lds<CX>(e_at(E, 0, row + 1, col));
             const Vec<CX> ey = lds<CX>(e_at(E, 1, row, col)), ez = lds<CX>(e_at(E, 2, row, col));
             const Vec<CX> ez_up = lds<CX>(e_at(E, 2, row + 1, col));
@@ -355,30 +436,44 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
                 ey_right = *e_at(E, 1, row, col + CX);
                 ez_right = *e_at(E, 2, row, col + CX);
             }
-            const Vec<CX> hx = lds<CX>(h_at(H, 0, row, col)), hy = lds<CX>(h_at(H, 1, row, col));
-            const Vec<CX> hz = lds<CX>(h_at(H, 2, row, col));
+            Vec<CX> nhx = lds<CX>(h_at(H, 0, row, col)), nhy = lds<CX>(h_at(H, 1, row, col));
+            Vec<CX> nhz = lds<CX>(h_at(H, 2, row, col));
+            uint32_t mat[CX];
+            load_materials<CX>(M + row * G::WM + mcol, mat);
             const float row_x = ahy + ahz, row_y = aiy + ahz, row_z = ahy + aiz;
-            Vec<CX> nhx, nhy, nhz;
+            float gain[CX], lx[CX], ly[CX], lz[CX], cx_[CX], cy_[CX], cz_[CX];
+            bool lossless = true;
 #pragma unroll
             for (int j = 0; j < CX; ++j) {
-                const float4 c = coeff[M[row * G::WM + mcol + j]];
+                const float4 c = coeff[mat[j]];
+                ecoef[j] = make_float2(c.x, c.y);
+                gain[j] = c.z;
                 const float eyr = j + 1 < CX ? ey.v[j + 1] : ey_right;
                 const float ezr = j + 1 < CX ? ez.v[j + 1] : ez_right;
-                const float curl_x = mgy * (ez_up.v[j] - ez.v[j]) - mgz * (ey_next.v[j] - ey.v[j]);
-                const float curl_y = mgz * (ex_next.v[j] - ex.v[j]) - mgx.v[j] * (ezr - ez.v[j]);
-                const float curl_z = mgx.v[j] * (eyr - ey.v[j]) - mgy * (ex_up.v[j] - ex.v[j]);
-                nhx.v[j] = h_update(hx.v[j], (c.w + row_x) + aix.v[j], c.z, curl_x);
-                nhy.v[j] = h_update(hy.v[j], (c.w + row_y) + ahx.v[j], c.z, curl_y);
-                nhz.v[j] = h_update(hz.v[j], (c.w + row_z) + ahx.v[j], c.z, curl_z);
+                cx_[j] = mgy * (ez_up.v[j] - ez.v[j]) - mgz * (ey_next.v[j] - ey.v[j]);
+                cy_[j] = mgz * (ex_next.v[j] - ex.v[j]) - mgx.v[j] * (ezr - ez.v[j]);
+                cz_[j] = mgx.v[j] * (eyr - ey.v[j]) - mgy * (ex_up.v[j] - ex.v[j]);
+                lx[j] = (c.w + row_x) + aix.v[j];
+                ly[j] = (c.w + row_y) + ahx.v[j];
+                lz[j] = (c.w + row_z) + ahx.v[j];
+                lossless = lossless && lx[j] == 0.0f && ly[j] == 0.0f && lz[j] == 0.0f;
             }
-            if (args.inj.count && touches(args.inj, true, y, p)) {
+            if (__all_sync(0xffffffffu, lossless)) {
 #pragma unroll
                 for (int j = 0; j < CX; ++j) {
-                    nhx.v[j] = inject(args.inj, s, true, 0, xl + j, y, p, nhx.v[j]);
-                    nhy.v[j] = inject(args.inj, s, true, 1, xl + j, y, p, nhy.v[j]);
-                    nhz.v[j] = inject(args.inj, s, true, 2, xl + j, y, p, nhz.v[j]);
+                    nhx.v[j] = nhx.v[j] - gain[j] * cx_[j];
+                    nhy.v[j] = nhy.v[j] - gain[j] * cy_[j];
+                    nhz.v[j] = nhz.v[j] - gain[j] * cz_[j];
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < CX; ++j) {
+                    nhx.v[j] = h_full(nhx.v[j], lx[j], gain[j], cx_[j]);
+                    nhy.v[j] = h_full(nhy.v[j], ly[j], gain[j], cy_[j]);
+                    nhz.v[j] = h_full(nhz.v[j], lz[j], gain[j], cz_[j]);
                 }
             }
+            if (mask_h) apply_injections<CX>(inj, s.weights, mask_h, xl, y, p, nhx, nhy, nhz);
             if (prologue) {
                 hx_prev = nhx;
                 hy_prev = nhy;
@@ -387,76 +482,34 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
                 sts<CX>(h_at(H, 1, row, col), nhy);
                 sts<CX>(h_at(H, 2, row, col), nhz);
                 if (store_row) {
-                    const uint64_t at = plane_base + uint64_t(y) * nx + xl;
                     stg<CX>(args.h_out + at, nhx);
                     stg<CX>(args.h_out + cells + at, nhy);
                     stg<CX>(args.h_out + 2 * cells + at, nhz);
                 }
             }
-        } else if (!prologue) {
-            // Halo row y0-1: the Hx and Hz that E at row y0 reads.
-            {
-                const int hr = 0, yy = y0 - 1;
-                const float hmgy = ldg_at(s.mgain + nx, yy, ny);
-                const float haiy = ldg_at(absorb_int + nx, yy, ny), hahy = ldg_at(absorb_half + nx, yy, ny);
-                const Vec<CX> ex = lds<CX>(e_at(E, 0, hr, col)), ex_up = lds<CX>(e_at(E, 0, hr + 1, col));
-                const Vec<CX> ey = lds<CX>(e_at(E, 1, hr, col)), ez = lds<CX>(e_at(E, 2, hr, col));
-                const Vec<CX> ez_up = lds<CX>(e_at(E, 2, hr + 1, col));
-                const Vec<CX> ey_next = lds<CX>(e_at(E1, 1, hr, col));
-                float ey_right = __shfl_down_sync(0xffffffffu, ey.v[0], 1);
-                if (lane == 31) ey_right = *e_at(E, 1, hr, col + CX);
-                const Vec<CX> hx = lds<CX>(h_at(H, 0, hr, col)), hz = lds<CX>(h_at(H, 2, hr, col));
-                const float row_x = hahy + ahz, row_z = hahy + aiz;
-                (void)haiy;
-                Vec<CX> nhx, nhz;
-#pragma unroll
-                for (int j = 0; j < CX; ++j) {
-                    const float4 c = coeff[M[hr * G::WM + mcol + j]];
-                    const float eyr = j + 1 < CX ? ey.v[j + 1] : ey_right;
-                    const float curl_x = hmgy * (ez_up.v[j] - ez.v[j]) - mgz * (ey_next.v[j] - ey.v[j]);
-                    const float curl_z = mgx.v[j] * (eyr - ey.v[j]) - hmgy * (ex_up.v[j] - ex.v[j]);
-                    nhx.v[j] = h_update(hx.v[j], (c.w + row_x) + aix.v[j], c.z, curl_x);
-                    nhz.v[j] = h_update(hz.v[j], (c.w + row_z) + ahx.v[j], c.z, curl_z);
-                }
-                if (args.inj.count && touches(args.inj, true, yy, p)) {
-#pragma unroll
-                    for (int j = 0; j < CX; ++j) {
-                        nhx.v[j] = inject(args.inj, s, true, 0, xl + j, yy, p, nhx.v[j]);
-                        nhz.v[j] = inject(args.inj, s, true, 2, xl + j, yy, p, nhz.v[j]);
-                    }
-                }
-                sts<CX>(h_at(H, 0, hr, col), nhx);
-                sts<CX>(h_at(H, 2, hr, col), nhz);
-            }
-            // Halo column x0-1, rows y0..y0+TY-1: the Hy and Hz that E at
-            // column x0 reads.
-            if (lane < kTileY) {
-                const int hr = hy_row, xx = x0 - 1, cc = 3;
-                const float ex = *e_at(E, 0, hr, cc), ex_up = *e_at(E, 0, hr + 1, cc);
-                const float ey = *e_at(E, 1, hr, cc), ez = *e_at(E, 2, hr, cc);
-                const float ex_next = *e_at(E1, 0, hr, cc);
-                const float eyr = *e_at(E, 1, hr, cc + 1), ezr = *e_at(E, 2, hr, cc + 1);
-                const float hy = *h_at(H, 1, hr, cc), hz = *h_at(H, 2, hr, cc);
-                const float4 c = coeff[M[hr * G::WM + 15]];
-                const float aix_h = ldg_at(absorb_int, xx, nx);
-                (void)aix_h;
-                const float curl_y = mgz * (ex_next - ex) - hc_mgx * (ezr - ez);
-                const float curl_z = hc_mgx * (eyr - ey) - hc_mgy * (ex_up - ex);
-                float nhy = h_update(hy, (c.w + (hc_aiy + ahz)) + hc_ahx, c.z, curl_y);
-                float nhz = h_update(hz, (c.w + (hc_ahy + aiz)) + hc_ahx, c.z, curl_z);
-                if (args.inj.count) {
-                    nhy = inject(args.inj, s, true, 1, xx, hy_y, p, nhy);
-                    nhz = inject(args.inj, s, true, 2, xx, hy_y, p, nhz);
-                }
-                *h_at(H, 1, hr, cc) = nhy;
-                *h_at(H, 2, hr, cc) = nhz;
-            }
         }
         if (prologue) continue; // CTA-uniform: nobody wrote shared memory
+
+        // ---------------- H(p): halo cells ----------------
+        if (halo_lane) {
+            const int hr = hc.hr, cc = hc.hc;
+            const float ex = *e_at(E, 0, hr, cc), ex_up = *e_at(E, 0, hr + 1, cc), ex_n = *e_at(E1, 0, hr, cc);
+            const float ey = *e_at(E, 1, hr, cc), ey_r = *e_at(E, 1, hr, cc + 1), ey_n = *e_at(E1, 1, hr, cc);
+            const float ez = *e_at(E, 2, hr, cc), ez_r = *e_at(E, 2, hr, cc + 1), ez_up = *e_at(E, 2, hr + 1, cc);
+            const float4 c = coeff[M[hr * G::WM + cc + 12]];
+            float nx_ = *h_at(H, 0, hr, cc), ny_ = *h_at(H, 1, hr, cc), nz_ = *h_at(H, 2, hr, cc);
+            nx_ = h_full(nx_, (c.w + (hc.ahy + ahz)) + hc.aix, c.z, hc.mgy * (ez_up - ez) - mgz * (ey_n - ey));
+            ny_ = h_full(ny_, (c.w + (hc.aiy + ahz)) + hc.ahx, c.z, mgz * (ex_n - ex) - hc.mgx * (ez_r - ez));
+            nz_ = h_full(nz_, (c.w + (hc.ahy + aiz)) + hc.ahx, c.z, hc.mgx * (ey_r - ey) - hc.mgy * (ex_up - ex));
+            if (hc.mask) apply_injections_1(inj, s.weights, hc.mask, hc.x, hc.y, p, nx_, ny_, nz_);
+            *h_at(H, 0, hr, cc) = nx_;
+            *h_at(H, 1, hr, cc) = ny_;
+            *h_at(H, 2, hr, cc) = nz_;
+        }
         __syncthreads();
 
         // ---------------- E(p) ----------------
-        if (!halo) {
+        {
             const Vec<CX> hx = lds<CX>(h_at(H, 0, row, col)), hy = lds<CX>(h_at(H, 1, row, col));
             const Vec<CX> hz = lds<CX>(h_at(H, 2, row, col));
             const Vec<CX> hx_dn = lds<CX>(h_at(H, 0, row - 1, col)), hz_dn = lds<CX>(h_at(H, 2, row - 1, col));
@@ -469,35 +522,48 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
             Vec<CX> ex = lds<CX>(e_at(E, 0, row, col)), ey = lds<CX>(e_at(E, 1, row, col));
             Vec<CX> ez = lds<CX>(e_at(E, 2, row, col));
             const float row_x = aiy + aiz, row_y = ahy + aiz, row_z = aiy + ahz;
+            float cx_[CX], cy_[CX], cz_[CX], lx[CX], ly[CX], lz[CX];
+            bool lossless = true;
 #pragma unroll
             for (int j = 0; j < CX; ++j) {
-                const int x = xl + j;
-                const float4 c = coeff[M[row * G::WM + mcol + j]];
                 const float hyl = j > 0 ? hy.v[j - 1] : hy_left;
                 const float hzl = j > 0 ? hz.v[j - 1] : hz_left;
-                if (y != 0 && p != 0) {
-                    const float curl = egy * (hz.v[j] - hz_dn.v[j]) - egz * (hy.v[j] - hy_prev.v[j]);
-                    ex.v[j] = e_update(ex.v[j], (c.y + row_x) + ahx.v[j], c.x, curl);
-                }
-                if (p != 0 && x != 0) {
-                    const float curl = egz * (hx.v[j] - hx_prev.v[j]) - egx.v[j] * (hz.v[j] - hzl);
-                    ey.v[j] = e_update(ey.v[j], (c.y + row_y) + aix.v[j], c.x, curl);
-                }
-                if (x != 0 && y != 0) {
-                    const float curl = egx.v[j] * (hy.v[j] - hyl) - egy * (hx.v[j] - hx_dn.v[j]);
-                    ez.v[j] = e_update(ez.v[j], (c.y + row_z) + aix.v[j], c.x, curl);
-                }
+                cx_[j] = egy * (hz.v[j] - hz_dn.v[j]) - egz * (hy.v[j] - hy_prev.v[j]);
+                cy_[j] = egz * (hx.v[j] - hx_prev.v[j]) - egx.v[j] * (hz.v[j] - hzl);
+                cz_[j] = egx.v[j] * (hy.v[j] - hyl) - egy * (hx.v[j] - hx_dn.v[j]);
+                lx[j] = (ecoef[j].y + row_x) + ahx.v[j];
+                ly[j] = (ecoef[j].y + row_y) + aix.v[j];
+                lz[j] = (ecoef[j].y + row_z) + aix.v[j];
+                lossless = lossless && lx[j] == 0.0f && ly[j] == 0.0f && lz[j] == 0.0f;
             }
-            if (args.inj.count && touches(args.inj, false, y, p)) {
+            Vec<CX> nex, ney, nez;
+            if (__all_sync(0xffffffffu, lossless)) {
 #pragma unroll
                 for (int j = 0; j < CX; ++j) {
-                    ex.v[j] = inject(args.inj, s, false, 0, xl + j, y, p, ex.v[j]);
-                    ey.v[j] = inject(args.inj, s, false, 1, xl + j, y, p, ey.v[j]);
-                    ez.v[j] = inject(args.inj, s, false, 2, xl + j, y, p, ez.v[j]);
+                    nex.v[j] = ex.v[j] + ecoef[j].x * cx_[j];
+                    ney.v[j] = ey.v[j] + ecoef[j].x * cy_[j];
+                    nez.v[j] = ez.v[j] + ecoef[j].x * cz_[j];
+                }
+            } else {
+#pragma unroll
+                for (int j = 0; j < CX; ++j) {
+                    nex.v[j] = e_full(ex.v[j], lx[j], ecoef[j].x, cx_[j]);
+                    ney.v[j] = e_full(ey.v[j], ly[j], ecoef[j].x, cy_[j]);
+                    nez.v[j] = e_full(ez.v[j], lz[j], ecoef[j].x, cz_[j]);
                 }
             }
+            // Index 0 along b or c is never written: the low-wall conductor
+            // (src/cpu.rs:386-394).
+            const bool update_x = y != 0 && p != 0;
+#pragma unroll
+            for (int j = 0; j < CX; ++j) {
+                const bool x_inner = xl + j != 0;
+                ex.v[j] = update_x ? nex.v[j] : ex.v[j];
+                ey.v[j] = (p != 0 && x_inner) ? ney.v[j] : ey.v[j];
+                ez.v[j] = (x_inner && y != 0) ? nez.v[j] : ez.v[j];
+            }
+            if (mask_e) apply_injections<CX>(inj, s.weights, mask_e, xl, y, p, ex, ey, ez);
             if (store_row) {
-                const uint64_t at = plane_base + uint64_t(y) * nx + xl;
                 stg<CX>(args.e_out + at, ex);
                 stg<CX>(args.e_out + cells + at, ey);
                 stg<CX>(args.e_out + 2 * cells + at, ez);
@@ -516,8 +582,8 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
             hy_prev = hy;
         }
     }
-    // Drain: every issued plane has been waited for (the loop waits through
-    // plane z1, the last one issued), so no copy is still landing here.
+    // Every issued plane has been waited for (the loop waits through plane
+    // z1, the last one issued), so no copy is still landing here.
 }
 
 // ---- host side ----------------------------------------------------------------
@@ -549,11 +615,30 @@ void encode(CUtensorMap *map, CUtensorMapDataType type, int rank, void *base, co
     if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed: " + std::to_string(int(r)));
 }
 
-template <int CX> void configure() {
+template <int CX, int TY, int SLOTS> void configure() {
     static bool done = false;
     if (done) return;
-    cudaFuncSetAttribute(fused_step<CX>, cudaFuncAttributeMaxDynamicSharedMemorySize, Geometry<CX>::SMEM);
+    cudaFuncSetAttribute(fused_step<CX, TY, SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         Geometry<CX, TY, SLOTS>::SMEM);
+    cudaFuncSetAttribute(fused_step<CX, TY, SLOTS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     done = true;
+}
+
+// The kernel variants this library carries: (cells per lane, rows per tile,
+// ring depth).  Each fits 16 resident warps per SM at 128 registers.
+struct Variant {
+    uint32_t cx, ty, slots;
+};
+constexpr Variant kVariants[] = {{4, 8, 3}, {2, 8, 5}, {4, 16, 3}, {1, 8, 5}};
+
+template <int CX, int TY, int SLOTS> size_t smem_of() { return Geometry<CX, TY, SLOTS>::SMEM; }
+
+size_t variant_smem(uint32_t cx, uint32_t ty, uint32_t slots) {
+    if (cx == 4 && ty == 8 && slots == 3) return smem_of<4, 8, 3>();
+    if (cx == 2 && ty == 8 && slots == 5) return smem_of<2, 8, 5>();
+    if (cx == 4 && ty == 16 && slots == 3) return smem_of<4, 16, 3>();
+    if (cx == 1 && ty == 8 && slots == 5) return smem_of<1, 8, 5>();
+    return 0;
 }
 
 int pick_cx(uint32_t nx) {
@@ -570,6 +655,14 @@ int pick_cx(uint32_t nx) {
     return best;
 }
 
+template <int CX, int TY, int SLOTS>
+void launch_variant(const FusedPlan &plan, const FusedMaps &m, const FusedArgs &args, cudaStream_t stream) {
+    configure<CX, TY, SLOTS>();
+    fused_step<CX, TY, SLOTS><<<plan.grid, 32 * TY, plan.smem, stream>>>(
+        *reinterpret_cast<const CUtensorMap *>(m.e), *reinterpret_cast<const CUtensorMap *>(m.h),
+        *reinterpret_cast<const CUtensorMap *>(m.m), args);
+}
+
 } // namespace
 
 bool fused_supported(const uint32_t n[3]) {
@@ -577,47 +670,60 @@ bool fused_supported(const uint32_t n[3]) {
     return n[0] % 4 == 0 && n[0] >= 4 && n[1] >= 2 && n[2] >= 2 && encoder() != nullptr;
 }
 
-FusedPlan fused_plan(const uint32_t n[3], uint32_t tile_y, uint32_t z_chunk, int sm_count) {
-    (void)tile_y;
+bool fused_variant_exists(uint32_t cx, uint32_t ty, uint32_t slots) { return variant_smem(cx, ty, slots) != 0; }
+
+FusedPlan fused_plan(const uint32_t n[3], uint32_t cx, uint32_t tile_y, uint32_t slots, uint32_t z_chunk,
+                     int sm_count) {
     FusedPlan p{};
-    p.tile_y = kTileY;
-    p.cx = pick_cx(n[0]);
+    p.cx = cx ? cx : uint32_t(pick_cx(n[0]));
+    p.tile_y = tile_y ? tile_y : 8;
+    p.slots = slots ? slots : (p.cx == 4 && p.tile_y == 8 ? 3 : (p.tile_y == 16 ? 3 : 5));
+    p.smem = variant_smem(p.cx, p.tile_y, p.slots);
+    if (p.smem == 0) throw std::runtime_error("no fused kernel variant with that tile shape and ring depth");
+    p.ctas_per_sm = 16 / p.tile_y;
     const uint32_t tx = 32u * p.cx;
     p.tiles_x = (n[0] + tx - 1) / tx;
-    p.tiles_y = (n[1] + kTileY - 1) / kTileY;
+    p.tiles_y = (n[1] + p.tile_y - 1) / p.tile_y;
     const uint32_t tiles = p.tiles_x * p.tiles_y;
     if (z_chunk == 0) {
-        // Enough chunks that the grid fills a few waves of two CTAs per SM,
-        // but no thinner than 16 planes (each chunk rebuilds one extra plane).
-        const uint32_t slots = 2u * uint32_t(sm_count > 0 ? sm_count : 1);
-        uint32_t chunks = (4 * slots + tiles - 1) / tiles;
-        chunks = chunks < 1 ? 1 : chunks;
-        z_chunk = (n[2] + chunks - 1) / chunks;
-        if (z_chunk < 16) z_chunk = 16;
+        // Pick the chunk depth whose CTA count fills whole waves best, among
+        // depths of at least 16 planes (each chunk rebuilds one extra plane).
+        const uint32_t resident = p.ctas_per_sm * uint32_t(sm_count > 0 ? sm_count : 1);
+        double best = 1e30;
+        z_chunk = n[2];
+        for (uint32_t depth = 16; depth <= n[2] + 15; ++depth) {
+            const uint32_t chunks = (n[2] + depth - 1) / depth;
+            const uint32_t waves = (tiles * chunks + resident - 1) / resident;
+            const double cost = double(waves) * double(depth + 1);
+            if (cost < best - 1e-9) {
+                best = cost;
+                z_chunk = depth;
+            }
+            if (depth >= n[2]) break;
+        }
     }
     p.z_chunk = z_chunk > n[2] ? n[2] : z_chunk;
     p.chunks = (n[2] + p.z_chunk - 1) / p.z_chunk;
     p.grid = tiles * p.chunks;
-    p.smem = p.cx == 4 ? Geometry<4>::SMEM : (p.cx == 2 ? Geometry<2>::SMEM : Geometry<1>::SMEM);
     return p;
 }
 
 void fused_maps(const DeviceScene &s, const FusedPlan &plan, FieldSet set, const uint8_t *material_padded,
                 uint32_t material_pitch, FusedMaps &out) {
-    const uint32_t tx = 32u * plan.cx;
+    const uint32_t tx = 32u * plan.cx, ty = plan.tile_y;
     const cuuint64_t nx = s.n[0], ny = s.n[1], nz = s.n[2];
     {
         cuuint64_t dims[4] = {nx, ny, nz, 3};
         cuuint64_t strides[3] = {nx * 4, nx * ny * 4, nx * ny * nz * 4};
-        cuuint32_t ebox[4] = {tx + 8, kTileY + 2, 1, 3};
-        cuuint32_t hbox[4] = {tx + 8, kTileY + 1, 1, 3};
+        cuuint32_t ebox[4] = {tx + 8, ty + 2, 1, 3};
+        cuuint32_t hbox[4] = {tx + 8, ty + 1, 1, 3};
         encode(reinterpret_cast<CUtensorMap *>(out.e), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, set.e, dims, strides, ebox);
         encode(reinterpret_cast<CUtensorMap *>(out.h), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, set.h, dims, strides, hbox);
     }
     {
         cuuint64_t dims[3] = {material_pitch, ny, nz};
         cuuint64_t strides[2] = {material_pitch, cuuint64_t(material_pitch) * ny};
-        cuuint32_t box[3] = {tx + 32, kTileY + 1, 1};
+        cuuint32_t box[3] = {tx + 32, ty + 1, 1};
         encode(reinterpret_cast<CUtensorMap *>(out.m), CU_TENSOR_MAP_DATA_TYPE_UINT8, 3,
                const_cast<uint8_t *>(material_padded), dims, strides, box);
     }
@@ -635,23 +741,10 @@ void launch_fused_step(const DeviceScene &s, const FusedPlan &plan, const FusedM
     args.tiles_y = plan.tiles_y;
     args.z_chunk = plan.z_chunk;
     args.inj = table;
-    const CUtensorMap &em = *reinterpret_cast<const CUtensorMap *>(in_maps.e);
-    const CUtensorMap &hm = *reinterpret_cast<const CUtensorMap *>(in_maps.h);
-    const CUtensorMap &mm = *reinterpret_cast<const CUtensorMap *>(in_maps.m);
-    switch (plan.cx) {
-    case 4:
-        configure<4>();
-        fused_step<4><<<plan.grid, kThreads, plan.smem, stream>>>(em, hm, mm, args);
-        break;
-    case 2:
-        configure<2>();
-        fused_step<2><<<plan.grid, kThreads, plan.smem, stream>>>(em, hm, mm, args);
-        break;
-    default:
-        configure<1>();
-        fused_step<1><<<plan.grid, kThreads, plan.smem, stream>>>(em, hm, mm, args);
-        break;
-    }
+    if (plan.cx == 4 && plan.tile_y == 8 && plan.slots == 3) launch_variant<4, 8, 3>(plan, in_maps, args, stream);
+    else if (plan.cx == 2 && plan.tile_y == 8 && plan.slots == 5) launch_variant<2, 8, 5>(plan, in_maps, args, stream);
+    else if (plan.cx == 4 && plan.tile_y == 16 && plan.slots == 3) launch_variant<4, 16, 3>(plan, in_maps, args, stream);
+    else launch_variant<1, 8, 5>(plan, in_maps, args, stream);
 }
 
 } // namespace diaphane

@@ -259,7 +259,12 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
     if (sim->kernel == DP_KERNEL_FUSED) {
         int sms = 0;
         check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sim->device), "attribute");
-        sim->plan = fused_plan(s.grid.n, opts ? opts->tile_y : 0, opts ? opts->z_chunk : 0, sms);
+        try {
+            sim->plan = fused_plan(s.grid.n, opts ? opts->cells_per_lane : 0, opts ? opts->tile_y : 0,
+                                   opts ? opts->ring_slots : 0, opts ? opts->z_chunk : 0, sms);
+        } catch (const std::exception &e) {
+            throw Error(DP_ERR_UNSUPPORTED, e.what());
+        }
         // The index again with rows padded to 16 bytes, for its tensor map.
         const uint32_t nx = s.grid.n[0], rows = s.grid.n[1] * s.grid.n[2];
         sim->material_pitch = (nx + 15) / 16 * 16;

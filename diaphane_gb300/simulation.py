@@ -93,10 +93,10 @@ class Simulation:
     """gpu::Simulation over the C ABI (one CUDA stream per handle)."""
 
     def __init__(self, scene: Scene | ResolvedScene, kernel: int = _abi.DP_KERNEL_AUTO, device: int = 0,
-                 tile_y: int = 0, z_chunk: int = 0):
+                 tile_y: int = 0, z_chunk: int = 0, cells_per_lane: int = 0, ring_slots: int = 0):
         self.resolved = scene if isinstance(scene, ResolvedScene) else ResolvedScene(scene)
         self.scene = self.resolved.scene
-        opts = _abi.dp_options(device, kernel, tile_y, z_chunk)
+        opts = _abi.dp_options(device, kernel, tile_y, z_chunk, cells_per_lane, ring_slots)
         handle = C.c_void_p()
         _abi.check(_abi.lib().dp_sim_create(self.resolved.handle, C.byref(opts), C.byref(handle)))
         self.handle = handle

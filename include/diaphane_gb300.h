@@ -235,10 +235,12 @@ enum {
 };
 
 typedef struct dp_options {
-    int32_t device;  /* CUDA ordinal */
-    uint32_t kernel; /* DP_KERNEL_* */
-    uint32_t tile_y; /* fused kernel rows per tile; 0 = tuned default */
-    uint32_t z_chunk;/* fused kernel planes per work unit; 0 = tuned default */
+    int32_t device;          /* CUDA ordinal */
+    uint32_t kernel;         /* DP_KERNEL_* */
+    uint32_t tile_y;         /* fused: rows per tile (8 or 16); 0 = default */
+    uint32_t z_chunk;        /* fused: planes per CTA; 0 = fill whole waves */
+    uint32_t cells_per_lane; /* fused: x cells per thread (1, 2 or 4); 0 = default */
+    uint32_t ring_slots;     /* fused: z-planes in the shared-memory ring; 0 = default */
 } dp_options;
 
 enum { DP_FIELD_ELECTRIC = 0, DP_FIELD_MAGNETIC = 1, DP_FIELD_INTENSITY = 2 };

@@ -149,3 +149,17 @@ def test_heterogeneous_workload_at_small_size_matches(threads):
         s.advance_by(300)
     assert np.array_equal(reference.read_electric().view(np.uint32), candidate.read_electric().view(np.uint32))
     assert np.array_equal(reference.read_intensity().view(np.uint32), candidate.read_intensity().view(np.uint32))
+
+
+@pytest.mark.parametrize("variant", [(4, 8, 3), (2, 8, 5), (4, 16, 3), (1, 8, 5)])
+@pytest.mark.parametrize("case", ["materials", "plane_wave", "several_sources"])
+def test_every_fused_variant_is_bit_identical(variant, case, threads):
+    """Tile width, tile height and ring depth are performance knobs only."""
+    scene, steps = scenes.PARITY_CASES[case]()
+    cx, ty, slots = variant
+    reference = oracle.OracleSimulation(scene, threads=threads)
+    candidate = Simulation(scene, kernel=DP_KERNEL_FUSED, cells_per_lane=cx, tile_y=ty, ring_slots=slots)
+    reference.advance_by(steps)
+    candidate.advance_by(steps)
+    assert np.array_equal(reference.read_electric().view(np.uint32), candidate.read_electric().view(np.uint32))
+    assert np.array_equal(reference.read_magnetic().view(np.uint32), candidate.read_magnetic().view(np.uint32))
