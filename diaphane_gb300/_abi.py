@@ -121,6 +121,7 @@ SIGNATURES = [
     ("dp_sim_energy", C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("dp_sim_is_finite", C.c_int, [_P, C.POINTER(C.c_int32)]),
     ("dp_sim_is_reversible", C.c_int32, [_P]),
+    ("dp_energy_noalloc", C.c_int, [_P, _P, _P, _P, _P, _P, C.POINTER(C.c_uint32), _P, _P]),
     ("dp_sim_kernel", C.c_uint32, [_P]),
     ("dp_sim_launch_count", C.c_uint64, [_P]),
 ]

@@ -289,6 +289,23 @@ dp_status dp_sim_energy(dp_sim *sim, double *electric, double *magnetic);
 dp_status dp_sim_is_finite(dp_sim *sim, int32_t *finite);
 /* is_reversible (src/cpu.rs:209-215). */
 int32_t dp_sim_is_reversible(const dp_sim *sim);
+/* Field energy of caller-owned device arrays, allocating nothing.  No
+ * counterpart in the reference: it exists for callers that cannot call
+ * cudaMalloc where they need the energy (cudaMalloc may synchronize the
+ * device or fail under memory pressure; some hosts own all device memory
+ * through their own allocator).  Computes what dp_sim_energy does, on the
+ * calling thread's current device and the given stream (NULL: default
+ * stream): electric/magnetic are 3*cells f32, material_index cells u8,
+ * eps_mu 2 f32 (relative permittivity, permeability) per material, primary
+ * and dual nx+ny+nz f32 each, out 2 f64 (electric, magnetic) — all device
+ * pointers.  Its partial sums live in a fixed 64 KiB array inside the
+ * library, so it covers at most 2^28 cells (DP_ERR_RANGE beyond).  The first
+ * call on a device looks that array's address up; make that first call
+ * before any stream capture.  Every call shares the array: calls whose
+ * kernels overlap on the GPU race and must be serialized by the caller. */
+dp_status dp_energy_noalloc(const float *electric, const float *magnetic, const uint8_t *material_index,
+                            const float *eps_mu, const float *primary, const float *dual,
+                            const uint32_t extent[3], double *out, void *stream);
 /* Kernel the handle actually runs (DP_KERNEL_FUSED or DP_KERNEL_NAIVE). */
 uint32_t dp_sim_kernel(const dp_sim *sim);
 /* Kernel launches issued by this handle so far (every kernel of this library). */
