@@ -43,6 +43,8 @@ def lib() -> C.CDLL:
             "or_sim_read_field64": (C.c_int, [P, C.c_int, P]),
             "or_sim_write_field": (C.c_int, [P, C.c_int, P]),
             "or_sim_restore": (C.c_int, [P, C.c_uint64, P, P]),
+            "or_sim_sample": (C.c_float, [P, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32]),
+            "or_sim_component": (C.c_int, [P, C.c_int, C.c_int, P]),
             "or_sim_energy": (None, [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
             "or_sim_is_finite": (C.c_int, [P]),
             "or_sim_extent": (None, [P, C.POINTER(C.c_uint32)]),
@@ -151,16 +153,22 @@ class OracleSimulation:
     def read_intensity(self, fp64: bool = False) -> np.ndarray:
         return self._read(_abi.DP_FIELD_INTENSITY, self.cells, fp64)
 
+    def _component(self, field: int, axis: int) -> np.ndarray:
+        out = np.empty(self.cells, dtype=np.float32)
+        _check(lib().or_sim_component(self.handle, field, int(axis), out.ctypes.data))
+        return out
+
     def electric(self, axis: int) -> np.ndarray:
-        a = int(axis)
-        return self.read_electric()[a * self.cells:(a + 1) * self.cells]
+        return self._component(_abi.DP_FIELD_ELECTRIC, axis)
 
     def magnetic(self, axis: int) -> np.ndarray:
-        a = int(axis)
-        return self.read_magnetic()[a * self.cells:(a + 1) * self.cells]
+        return self._component(_abi.DP_FIELD_MAGNETIC, axis)
 
     def sample_electric(self, axis: int, coord) -> float:
-        return float(self.electric(axis)[self.index(coord)])
+        return lib().or_sim_sample(self.handle, _abi.DP_FIELD_ELECTRIC, int(axis), *[int(c) for c in coord])
+
+    def sample_magnetic(self, axis: int, coord) -> float:
+        return lib().or_sim_sample(self.handle, _abi.DP_FIELD_MAGNETIC, int(axis), *[int(c) for c in coord])
 
     def index(self, coord) -> int:
         return (coord[2] * self.extent[1] + coord[1]) * self.extent[0] + coord[0]

@@ -1024,6 +1024,29 @@ int or_sim_restore(or_sim *s, uint64_t step, const float *electric, const float 
     return 0;
 }
 
+// One value, or one component, of a field (sample_electric and friends,
+// src/cpu.rs:136-160).
+float or_sim_sample(const or_sim *s, int field, int component, uint32_t x, uint32_t y, uint32_t z) {
+    auto sample = [&](auto *sim) -> float {
+        size_t i = sim->grid.index(x, y, z);
+        if (field == DP_FIELD_INTENSITY) return float(sim->intensity[i]);
+        auto &f = field == DP_FIELD_ELECTRIC ? sim->electric : sim->magnetic;
+        return float(f[component][i]);
+    };
+    return s->f32 ? sample(s->f32) : sample(s->f64);
+}
+
+int or_sim_component(const or_sim *s, int field, int component, float *out) {
+    auto read = [&](auto *sim) {
+        size_t n = sim->grid.total();
+        auto &f = field == DP_FIELD_ELECTRIC ? sim->electric : sim->magnetic;
+        for (size_t i = 0; i < n; ++i) out[i] = float(f[component][i]);
+    };
+    if (s->f32) read(s->f32);
+    else read(s->f64);
+    return 0;
+}
+
 void or_sim_energy(const or_sim *s, double *electric, double *magnetic) {
     if (s->f32) s->f32->energy(electric, magnetic);
     else s->f64->energy(electric, magnetic);
