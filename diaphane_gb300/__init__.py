@@ -8,10 +8,11 @@ from ._abi import DiaphaneError, DP_KERNEL_AUTO, DP_KERNEL_FUSED, DP_KERNEL_NAIV
 from .scene import (Axis, Boundary, Extent, Grid, Material, MaterialTable, Refinement, Scene, Shape, Source,
                     Waveform, COURANT_LIMIT, SPEED_OF_LIGHT)
 from .simulation import Energy, ResolvedScene, Simulation, Snapshot
+from .batch import Batch
 from .timeline import Seek, Timeline
 
 __all__ = [
-    "Axis", "Boundary", "COURANT_LIMIT", "DiaphaneError", "DP_KERNEL_AUTO", "DP_KERNEL_FUSED", "DP_KERNEL_NAIVE",
+    "Axis", "Batch", "Boundary", "COURANT_LIMIT", "DiaphaneError", "DP_KERNEL_AUTO", "DP_KERNEL_FUSED", "DP_KERNEL_NAIVE",
     "Energy", "Extent", "Grid", "Material", "MaterialTable", "Refinement", "ResolvedScene", "Scene", "Seek",
     "Shape", "Simulation", "Snapshot", "SPEED_OF_LIGHT", "Source", "Timeline", "Waveform",
 ]

@@ -84,6 +84,11 @@ class dp_injection(C.Structure):
                 ("value", C.c_float), ("inverse_waist_squared", C.c_float), ("center", F3)]
 
 
+class dp_batch_options(C.Structure):
+    _fields_ = [("device", C.c_int32), ("chunk_steps", C.c_uint32), ("arena_bytes", C.c_uint64),
+                ("max_scenes", C.c_uint32), ("use_graphs", C.c_uint32)]
+
+
 class dp_options(C.Structure):
     _fields_ = [("device", C.c_int32), ("kernel", C.c_uint32), ("tile_y", C.c_uint32), ("z_chunk", C.c_uint32),
                 ("cells_per_lane", C.c_uint32), ("ring_slots", C.c_uint32)]
@@ -121,6 +126,19 @@ SIGNATURES = [
     ("dp_sim_energy", C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("dp_sim_is_finite", C.c_int, [_P, C.POINTER(C.c_int32)]),
     ("dp_sim_is_reversible", C.c_int32, [_P]),
+    ("dp_batch_create", C.c_int, [C.POINTER(dp_batch_options), C.POINTER(_P)]),
+    ("dp_batch_destroy", None, [_P]),
+    ("dp_batch_add", C.c_int, [_P, _P, C.c_uint64, C.c_int32, C.POINTER(C.c_uint32), C.c_uint32,
+                               C.POINTER(C.c_uint64)]),
+    ("dp_batch_remove", C.c_int, [_P, C.c_uint64]),
+    ("dp_batch_advance_chunk", C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    ("dp_batch_wait", C.c_int, [_P, C.c_uint32]),
+    ("dp_batch_status", C.c_int, [_P, C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("dp_batch_read_field", C.c_int, [_P, C.c_uint64, C.c_uint32, _P, C.c_size_t]),
+    ("dp_batch_read_probes", C.c_int, [_P, C.c_uint64, _P, C.c_size_t]),
+    ("dp_batch_memory", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("dp_scene_batch_bytes", C.c_uint64, [_P, C.c_uint32, C.c_uint64]),
+    ("dp_batch_launch_count", C.c_uint64, [_P]),
     ("dp_energy_noalloc", C.c_int, [_P, _P, _P, _P, _P, _P, C.POINTER(C.c_uint32), _P, _P]),
     ("dp_sim_kernel", C.c_uint32, [_P]),
     ("dp_sim_launch_count", C.c_uint64, [_P]),

@@ -1,0 +1,666 @@
+// The batched form: many scenes of uneven sizes advanced together.
+//
+// Every scene lives in one device arena (fields, intensity, padded material
+// index, tables), admitted by bytes against the arena's capacity.  A step of
+// the whole batch is one launch per kernel variant over a work list of
+// (scene, tile, z-chunk) units drawn from all scenes; a chunk of K steps is
+// captured once into a CUDA graph and replayed while the batch's membership
+// is unchanged.  What changes from chunk to chunk — each scene's injections
+// for each step, how many steps it takes, which field set is current — lives
+// in device tables the host rewrites before each replay, so the graph's
+// topology never depends on scene content.  Scenes join and leave only
+// between chunks; a scene that finishes mid-chunk sits out the rest of it.
+#include "abi.hpp"
+#include "device.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <thread>
+#include <vector>
+
+namespace diaphane {
+const Scene &scene_of(const dp_scene *s);
+}
+
+using namespace diaphane;
+
+namespace {
+
+void check(cudaError_t err, const char *what) {
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        throw Error(err == cudaErrorMemoryAllocation ? DP_ERR_OOM : DP_ERR_CUDA,
+                    std::string(what) + ": " + cudaGetErrorString(err));
+    }
+}
+
+constexpr size_t kAlign = 256;
+
+size_t round_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+// First-fit allocator over the arena's byte range.
+class Arena {
+  public:
+    void reset(size_t capacity) {
+        free_.clear();
+        free_[0] = capacity;
+        used_ = 0;
+        capacity_ = capacity;
+    }
+    bool allocate(size_t bytes, size_t &offset) {
+        bytes = round_up(bytes, kAlign);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= bytes) {
+                offset = it->first;
+                const size_t rest = it->second - bytes;
+                free_.erase(it);
+                if (rest) free_[offset + bytes] = rest;
+                used_ += bytes;
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t offset, size_t bytes) {
+        bytes = round_up(bytes, kAlign);
+        used_ -= bytes;
+        auto next = free_.lower_bound(offset);
+        if (next != free_.end() && offset + bytes == next->first) {
+            bytes += next->second;
+            next = free_.erase(next);
+        }
+        if (next != free_.begin()) {
+            auto prev = std::prev(next);
+            if (prev->first + prev->second == offset) {
+                prev->second += bytes;
+                return;
+            }
+        }
+        free_[offset] = bytes;
+    }
+    size_t used() const { return used_; }
+    size_t capacity() const { return capacity_; }
+
+  private:
+    std::map<size_t, size_t> free_;
+    size_t used_ = 0, capacity_ = 0;
+};
+
+struct Variant {
+    uint32_t cx, tile_y, slots;
+    bool operator==(const Variant &o) const { return cx == o.cx && tile_y == o.tile_y && slots == o.slots; }
+};
+
+// The variant a grid shape runs: the widest tile that wastes no more lanes
+// than a narrower one, 8 rows, and the ring depth that variant is built with.
+Variant variant_for(uint32_t nx) {
+    uint32_t best = 4, waste_best = ~0u;
+    for (uint32_t cx : {4u, 2u, 1u}) {
+        const uint32_t tx = 32 * cx, waste = (nx + tx - 1) / tx * tx - nx;
+        if (waste < waste_best) {
+            best = cx;
+            waste_best = waste;
+        }
+    }
+    return Variant{best, 8, best == 4 ? 3u : 5u};
+}
+
+struct Entry {
+    uint64_t id = 0;
+    Scene scene;
+    uint32_t slot = 0;            // index into the descriptor array
+    Variant variant{};
+    uint32_t pitch = 0, material_pitch = 0;
+    uint64_t cells_padded = 0;
+    size_t offset = 0, bytes = 0; // arena block
+    BatchScene desc{};
+    uint64_t step = 0;            // steps completed
+    uint64_t target = 0;          // steps requested
+    bool accumulate = false;
+    std::vector<uint32_t> probe_cells; // padded linear cell index per probe
+    float *probes = nullptr;      // target × probes × 2 (Ez, Hy)
+    std::vector<BatchUnit> units;
+};
+
+// Per-step probe gather: after step t of a chunk, Ez and Hy at every probe
+// of every scene still stepping.
+struct ProbeSlot {
+    uint32_t slot;      // scene descriptor index
+    uint32_t k;         // probe number within the scene
+    uint32_t probes;    // probes of that scene
+    uint32_t cell;      // padded linear index
+    float *series;      // the scene's probe series
+};
+
+__global__ void gather_probes(const BatchScene *scenes, const ProbeSlot *slots, uint32_t count, uint32_t step) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    const ProbeSlot ps = slots[i];
+    const BatchScene &bs = scenes[ps.slot];
+    if (step >= bs.steps) return;
+    const uint32_t out = (bs.parity + step + 1u) & 1u; // the set this step wrote
+    const float ez = bs.e[out][2 * bs.s.cells + ps.cell];
+    const float hy = bs.h[out][bs.s.cells + ps.cell];
+    const uint64_t at = ((bs.step0 + step) * ps.probes + ps.k) * 2;
+    ps.series[at] = ez;
+    ps.series[at + 1] = hy;
+}
+
+} // namespace
+
+struct dp_batch {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint32_t chunk = 50;
+    uint32_t capacity = 0;        // scene slots
+    bool graphs = true;
+    unsigned char *arena_base = nullptr;
+    Arena arena;
+    std::map<uint64_t, Entry> entries;
+    std::vector<int> slot_used;
+    uint64_t next_id = 1;
+    // Device tables.
+    BatchScene *scenes = nullptr;                 // [capacity]
+    DeviceInjection *injections = nullptr;        // [2][chunk][capacity][kBatchInjections]
+    uint32_t *counts = nullptr;                   // [2][chunk][capacity]
+    std::vector<BatchUnit *> units;               // per variant
+    std::vector<uint32_t> unit_counts;
+    std::vector<Variant> variants;
+    ProbeSlot *probe_slots = nullptr;
+    uint32_t probe_count = 0;
+    int32_t *error = nullptr;
+    // Host staging (pinned), double-buffered against in-flight copies.
+    BatchScene *h_scenes[2] = {nullptr, nullptr};
+    DeviceInjection *h_injections[2] = {nullptr, nullptr};
+    uint32_t *h_counts[2] = {nullptr, nullptr};
+    cudaEvent_t staged[2] = {nullptr, nullptr};
+    int stage = 0;
+    // Graph of one chunk, rebuilt when the work lists change.
+    bool dirty = true;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr}; // one per staging half
+    uint64_t launches = 0;
+    uint64_t chunks_run = 0;
+
+    void bind() { check(cudaSetDevice(device), "cudaSetDevice"); }
+
+    ~dp_batch() {
+        if (stream) {
+            cudaSetDevice(device);
+            cudaStreamSynchronize(stream);
+        }
+        for (auto &e : exec)
+            if (e) cudaGraphExecDestroy(e);
+        for (BatchUnit *u : units) cudaFree(u);
+        cudaFree(scenes);
+        cudaFree(injections);
+        cudaFree(counts);
+        cudaFree(probe_slots);
+        cudaFree(error);
+        cudaFree(arena_base);
+        for (int k = 0; k < 2; ++k) {
+            cudaFreeHost(h_scenes[k]);
+            cudaFreeHost(h_injections[k]);
+            cudaFreeHost(h_counts[k]);
+            if (staged[k]) cudaEventDestroy(staged[k]);
+        }
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    size_t injection_span() const { return size_t(chunk) * capacity * kBatchInjections; }
+    size_t count_span() const { return size_t(chunk) * capacity; }
+
+    // Work lists and probe slots from the current membership.
+    void rebuild_lists() {
+        // The previous chunk may still be reading the old lists.
+        check(cudaStreamSynchronize(stream), "previous chunk");
+        for (BatchUnit *u : units) cudaFree(u);
+        units.clear();
+        unit_counts.clear();
+        variants.clear();
+        std::vector<std::vector<BatchUnit>> lists;
+        std::vector<ProbeSlot> probes;
+        for (auto &kv : entries) {
+            Entry &e = kv.second;
+            size_t v = 0;
+            while (v < variants.size() && !(variants[v] == e.variant)) ++v;
+            if (v == variants.size()) {
+                variants.push_back(e.variant);
+                lists.emplace_back();
+            }
+            lists[v].insert(lists[v].end(), e.units.begin(), e.units.end());
+            for (uint32_t k = 0; k < e.probe_cells.size(); ++k)
+                probes.push_back(ProbeSlot{e.slot, k, uint32_t(e.probe_cells.size()), e.probe_cells[k], e.probes});
+        }
+        for (auto &list : lists) {
+            BatchUnit *d = nullptr;
+            check(cudaMalloc(&d, std::max<size_t>(1, list.size()) * sizeof(BatchUnit)), "cudaMalloc units");
+            check(cudaMemcpyAsync(d, list.data(), list.size() * sizeof(BatchUnit), cudaMemcpyHostToDevice, stream),
+                  "units");
+            units.push_back(d);
+            unit_counts.push_back(uint32_t(list.size()));
+        }
+        cudaFree(probe_slots);
+        probe_slots = nullptr;
+        probe_count = uint32_t(probes.size());
+        check(cudaMalloc(&probe_slots, std::max<size_t>(1, probes.size()) * sizeof(ProbeSlot)), "cudaMalloc probes");
+        if (!probes.empty())
+            check(cudaMemcpyAsync(probe_slots, probes.data(), probes.size() * sizeof(ProbeSlot),
+                                  cudaMemcpyHostToDevice, stream),
+                  "probe slots");
+        check(cudaStreamSynchronize(stream), "work lists");
+        for (auto &x : exec)
+            if (x) {
+                cudaGraphExecDestroy(x);
+                x = nullptr;
+            }
+        dirty = false;
+    }
+
+    // The launches of one chunk reading staging half `half`.
+    void record_chunk(int half) {
+        const DeviceInjection *inj = injections + size_t(half) * injection_span();
+        const uint32_t *cnt = counts + size_t(half) * count_span();
+        for (uint32_t t = 0; t < chunk; ++t) {
+            for (size_t v = 0; v < variants.size(); ++v) {
+                launch_batch_step(variants[v].cx, variants[v].tile_y, variants[v].slots, scenes, units[v],
+                                  unit_counts[v], inj, cnt, capacity, t, error, stream);
+                ++launches;
+            }
+            if (probe_count) {
+                gather_probes<<<(probe_count + 255) / 256, 256, 0, stream>>>(scenes, probe_slots, probe_count, t);
+                ++launches;
+            }
+        }
+    }
+
+    // One chunk: stage descriptors and injections, then replay (or launch).
+    uint32_t run_chunk() {
+        if (dirty) rebuild_lists();
+        const int half = stage;
+        // The staging half is free once the copies that last read it are done.
+        check(cudaEventSynchronize(staged[half]), "staging");
+        BatchScene *hs = h_scenes[half];
+        DeviceInjection *hi = h_injections[half];
+        uint32_t *hc = h_counts[half];
+        std::memset(hc, 0, count_span() * sizeof(uint32_t));
+        uint32_t stepping = 0;
+        std::vector<StepInjection> step_injections;
+        std::vector<ProbeSlot> probe_updates;
+        for (auto &kv : entries) {
+            Entry &e = kv.second;
+            const uint64_t remaining = e.target > e.step ? e.target - e.step : 0;
+            const uint32_t steps = uint32_t(std::min<uint64_t>(remaining, chunk));
+            e.desc.steps = steps;
+            e.desc.parity = uint32_t(e.step & 1u);
+            e.desc.step0 = e.step;
+            hs[e.slot] = e.desc;
+            if (steps) ++stepping;
+            for (uint32_t t = 0; t < steps; ++t) {
+                const float time = float(e.step + t + 1) * e.scene.dt;
+                e.scene.injections(time, step_injections);
+                uint32_t n = 0;
+                DeviceInjection *row = hi + (size_t(t) * capacity + e.slot) * kBatchInjections;
+                for (const StepInjection &si : step_injections) {
+                    if (si.value == 0.0f) continue;
+                    if (n == kBatchInjections) throw Error(DP_ERR_UNSUPPORTED, "too many injections for a batch scene");
+                    DeviceInjection &d = row[n++];
+                    for (int a = 0; a < 3; ++a) {
+                        d.origin[a] = si.origin[a];
+                        d.extent[a] = si.extent[a];
+                    }
+                    d.component = si.component;
+                    d.magnetic = si.magnetic;
+                    d.value = si.value;
+                    d.weight_offset = si.weight_offset;
+                }
+                hc[size_t(t) * capacity + e.slot] = n;
+            }
+        }
+        check(cudaMemcpyAsync(scenes, hs, size_t(capacity) * sizeof(BatchScene), cudaMemcpyHostToDevice, stream),
+              "descriptors");
+        check(cudaMemcpyAsync(injections + size_t(half) * injection_span(), hi,
+                              injection_span() * sizeof(DeviceInjection), cudaMemcpyHostToDevice, stream),
+              "injections");
+        check(cudaMemcpyAsync(counts + size_t(half) * count_span(), hc, count_span() * sizeof(uint32_t),
+                              cudaMemcpyHostToDevice, stream),
+              "counts");
+        check(cudaEventRecord(staged[half], stream), "staging event");
+        if (stepping) {
+            if (graphs) {
+                if (!exec[half]) {
+                    cudaGraph_t graph = nullptr;
+                    check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "capture");
+                    const uint64_t before = launches;
+                    record_chunk(half);
+                    check(cudaStreamEndCapture(stream, &graph), "capture");
+                    launches = before;
+                    check(cudaGraphInstantiate(&exec[half], graph, 0), "instantiate");
+                    cudaGraphDestroy(graph);
+                }
+                check(cudaGraphLaunch(exec[half], stream), "graph launch");
+                launches += uint64_t(chunk) * (variants.size() + (probe_count ? 1 : 0));
+            } else {
+                record_chunk(half);
+            }
+            check(cudaGetLastError(), "chunk launch");
+        }
+        for (auto &kv : entries) {
+            Entry &e = kv.second;
+            e.step += e.desc.steps;
+        }
+        stage ^= 1;
+        ++chunks_run;
+        return stepping;
+    }
+
+    void wait(uint32_t timeout_ms) {
+        const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
+        for (;;) {
+            cudaError_t q = cudaStreamQuery(stream);
+            if (q == cudaSuccess) break;
+            if (q != cudaErrorNotReady) check(q, "stream");
+            if (std::chrono::steady_clock::now() >= deadline) throw Error(DP_ERR_TIMEOUT, "the batch did not finish in time");
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+        }
+        int32_t code = 0;
+        check(cudaMemcpy(&code, error, sizeof(code), cudaMemcpyDeviceToHost), "error flag");
+        if (code) {
+            check(cudaMemset(error, 0, sizeof(int32_t)), "error flag");
+            throw Error(DP_ERR_TIMEOUT, "a batch step gave up waiting for its plane loads");
+        }
+    }
+};
+
+namespace {
+
+constexpr uint32_t kTimeoutMs = 600000;
+
+// Bytes a scene needs in the arena.
+struct Layout {
+    uint32_t pitch, material_pitch;
+    uint64_t cells;
+    size_t fields, intensity, material, coeff, gains, absorber, weights, probes, total;
+};
+
+Layout layout_of(const Scene &s, uint32_t probe_count, uint64_t steps) {
+    Layout l{};
+    const uint32_t *n = s.grid.n;
+    l.pitch = (n[0] + 3) / 4 * 4;
+    l.material_pitch = (n[0] + 15) / 16 * 16;
+    l.cells = uint64_t(l.pitch) * n[1] * n[2];
+    const size_t span = size_t(n[0]) + n[1] + n[2];
+    l.fields = round_up(3 * l.cells * sizeof(float), kAlign);
+    l.intensity = round_up(l.cells * sizeof(float), kAlign);
+    l.material = round_up(size_t(l.material_pitch) * n[1] * n[2], kAlign);
+    l.coeff = round_up(256 * sizeof(float4), kAlign);
+    l.gains = round_up(span * sizeof(float), kAlign);
+    l.absorber = round_up(2 * span * sizeof(float), kAlign);
+    l.weights = round_up(std::max<size_t>(1, s.weights.size()) * sizeof(float), kAlign);
+    l.probes = round_up(std::max<size_t>(1, size_t(probe_count) * steps * 2) * sizeof(float), kAlign);
+    l.total = 4 * l.fields + l.intensity + l.material + l.coeff + 2 * l.gains + l.absorber + l.weights + l.probes;
+    return l;
+}
+
+void make_units(Entry &e, int sm_count) {
+    const uint32_t *n = e.scene.grid.n;
+    const uint32_t tx = 32 * e.variant.cx, ty = e.variant.tile_y;
+    const uint32_t tiles_x = (n[0] + tx - 1) / tx, tiles_y = (n[1] + ty - 1) / ty;
+    // Units of about 24 planes: enough planes to amortize a unit's start-up
+    // (one extra H plane, ring fill), small enough to spread a scene.
+    (void)sm_count;
+    const uint32_t depth = std::max<uint32_t>(8, std::min<uint32_t>(24, n[2]));
+    e.units.clear();
+    for (uint32_t z0 = 0; z0 < n[2]; z0 += depth)
+        for (uint32_t ty_i = 0; ty_i < tiles_y; ++ty_i)
+            for (uint32_t tx_i = 0; tx_i < tiles_x; ++tx_i)
+                e.units.push_back(BatchUnit{e.slot, tx_i * tx, ty_i * ty, z0, std::min(z0 + depth, n[2])});
+}
+
+} // namespace
+
+extern "C" {
+
+dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out) {
+    return guarded([&] {
+        if (!opts || !out) throw Error(DP_ERR_INVALID, "null argument");
+        *out = nullptr;
+        auto b = std::make_unique<dp_batch>();
+        b->device = opts->device;
+        b->chunk = opts->chunk_steps ? opts->chunk_steps : 50;
+        b->capacity = opts->max_scenes ? opts->max_scenes : 256;
+        b->graphs = opts->use_graphs != 0;
+        if (opts->arena_bytes == 0) throw Error(DP_ERR_INVALID, "arena_bytes must be positive");
+        b->bind();
+        check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
+        configure_batch_kernels();
+        check(cudaMalloc(&b->arena_base, opts->arena_bytes), "arena");
+        b->arena.reset(opts->arena_bytes);
+        b->slot_used.assign(b->capacity, 0);
+        check(cudaMalloc(&b->scenes, size_t(b->capacity) * sizeof(BatchScene)), "descriptors");
+        check(cudaMemset(b->scenes, 0, size_t(b->capacity) * sizeof(BatchScene)), "descriptors");
+        check(cudaMalloc(&b->injections, 2 * b->injection_span() * sizeof(DeviceInjection)), "injections");
+        check(cudaMalloc(&b->counts, 2 * b->count_span() * sizeof(uint32_t)), "counts");
+        check(cudaMemset(b->counts, 0, 2 * b->count_span() * sizeof(uint32_t)), "counts");
+        check(cudaMalloc(&b->error, sizeof(int32_t)), "error");
+        check(cudaMemset(b->error, 0, sizeof(int32_t)), "error");
+        for (int k = 0; k < 2; ++k) {
+            check(cudaMallocHost(&b->h_scenes[k], size_t(b->capacity) * sizeof(BatchScene)), "staging");
+            std::memset(b->h_scenes[k], 0, size_t(b->capacity) * sizeof(BatchScene));
+            check(cudaMallocHost(&b->h_injections[k], b->injection_span() * sizeof(DeviceInjection)), "staging");
+            check(cudaMallocHost(&b->h_counts[k], b->count_span() * sizeof(uint32_t)), "staging");
+            check(cudaEventCreateWithFlags(&b->staged[k], cudaEventDisableTiming), "event");
+            check(cudaEventRecord(b->staged[k], b->stream), "event");
+        }
+        *out = b.release();
+        return DP_OK;
+    });
+}
+
+void dp_batch_destroy(dp_batch *batch) { delete batch; }
+
+dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32_t accumulate_intensity,
+                       const uint32_t *probes, uint32_t probe_count, uint64_t *id) {
+    return guarded([&] {
+        if (!b || !scene || !id || (probe_count && !probes)) throw Error(DP_ERR_INVALID, "null argument");
+        const Scene &s = scene_of(scene);
+        if (!tensor_maps_available()) throw Error(DP_ERR_UNSUPPORTED, "the driver offers no tensor-map encoder");
+        if (2 * s.sources.size() > size_t(kBatchInjections))
+            throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 4 sources");
+        uint32_t slot = 0;
+        while (slot < b->capacity && b->slot_used[slot]) ++slot;
+        if (slot == b->capacity) throw Error(DP_ERR_BUSY, "every scene slot of the batch is in use");
+        const Layout l = layout_of(s, probe_count, steps);
+        size_t offset = 0;
+        if (!b->arena.allocate(l.total, offset)) throw Error(DP_ERR_OOM, "the batch arena cannot hold this scene now");
+        b->bind();
+        Entry e;
+        e.id = b->next_id++;
+        e.scene = s;
+        e.slot = slot;
+        e.variant = variant_for(s.grid.n[0]);
+        e.pitch = l.pitch;
+        e.material_pitch = l.material_pitch;
+        e.cells_padded = l.cells;
+        e.offset = offset;
+        e.bytes = l.total;
+        e.target = steps;
+        e.accumulate = accumulate_intensity != 0;
+        unsigned char *p = b->arena_base + offset;
+        auto take = [&](size_t bytes) {
+            unsigned char *q = p;
+            p += bytes;
+            return q;
+        };
+        BatchScene &d = e.desc;
+        std::memset(&d, 0, sizeof(d));
+        for (int k = 0; k < 2; ++k) {
+            d.e[k] = reinterpret_cast<float *>(take(l.fields));
+            d.h[k] = reinterpret_cast<float *>(take(l.fields));
+        }
+        float *intensity = reinterpret_cast<float *>(take(l.intensity));
+        uint8_t *material = take(l.material);
+        float4 *coeff = reinterpret_cast<float4 *>(take(l.coeff));
+        float *mgain = reinterpret_cast<float *>(take(l.gains));
+        float *egain = reinterpret_cast<float *>(take(l.gains));
+        float *absorber = reinterpret_cast<float *>(take(l.absorber));
+        float *weights = reinterpret_cast<float *>(take(l.weights));
+        e.probes = reinterpret_cast<float *>(take(l.probes));
+        // Zeroed fields; tables uploaded; the index padded row by row.
+        cudaStream_t st = b->stream;
+        check(cudaMemsetAsync(b->arena_base + offset, 0, 4 * l.fields + l.intensity, st), "zero fields");
+        const uint32_t nx = s.grid.n[0], rows = s.grid.n[1] * s.grid.n[2];
+        std::vector<uint8_t> padded(size_t(l.material_pitch) * rows, 0);
+        for (size_t r = 0; r < rows; ++r) std::memcpy(&padded[r * l.material_pitch], &s.material_index[r * nx], nx);
+        check(cudaMemcpyAsync(material, padded.data(), padded.size(), cudaMemcpyHostToDevice, st), "index");
+        std::vector<float4> table(256, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        for (size_t m = 0; m < s.coefficients.size(); ++m)
+            table[m] = make_float4(s.coefficients[m].electric_gain, s.coefficients[m].electric_loss,
+                                   s.coefficients[m].magnetic_gain, s.coefficients[m].magnetic_loss);
+        check(cudaMemcpyAsync(coeff, table.data(), table.size() * sizeof(float4), cudaMemcpyHostToDevice, st), "coeff");
+        check(cudaMemcpyAsync(mgain, s.magnetic_gains.data(), s.magnetic_gains.size() * 4, cudaMemcpyHostToDevice, st), "gains");
+        check(cudaMemcpyAsync(egain, s.electric_gains.data(), s.electric_gains.size() * 4, cudaMemcpyHostToDevice, st), "gains");
+        check(cudaMemcpyAsync(absorber, s.absorber.data(), s.absorber.size() * 4, cudaMemcpyHostToDevice, st), "absorber");
+        if (!s.weights.empty())
+            check(cudaMemcpyAsync(weights, s.weights.data(), s.weights.size() * 4, cudaMemcpyHostToDevice, st), "weights");
+        check(cudaStreamSynchronize(st), "scene upload");
+        for (int a = 0; a < 3; ++a) d.s.n[a] = s.grid.n[a];
+        d.s.pitch = l.pitch;
+        d.s.cells = l.cells;
+        d.s.material = nullptr; // the fused step reads the index through its tensor map
+        d.s.coeff = coeff;
+        d.s.mgain = mgain;
+        d.s.egain = egain;
+        d.s.absorber = absorber;
+        d.s.weights = weights;
+        d.intensity = e.accumulate ? intensity : nullptr;
+        try {
+            batch_scene_maps(d, e.variant.cx, e.variant.tile_y, material, l.material_pitch);
+        } catch (const std::exception &ex) {
+            b->arena.release(offset, l.total);
+            throw Error(DP_ERR_CUDA, ex.what());
+        }
+        for (uint32_t k = 0; k < probe_count; ++k) {
+            const uint32_t *c = probes + 3 * k;
+            if (c[0] >= s.grid.n[0] || c[1] >= s.grid.n[1] || c[2] >= s.grid.n[2]) {
+                b->arena.release(offset, l.total);
+                throw Error(DP_ERR_RANGE, "probe outside the grid");
+            }
+            e.probe_cells.push_back(uint32_t((uint64_t(c[2]) * s.grid.n[1] + c[1]) * l.pitch + c[0]));
+        }
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
+        make_units(e, sms);
+        b->slot_used[slot] = 1;
+        *id = e.id;
+        b->entries.emplace(e.id, std::move(e));
+        b->dirty = true;
+        return DP_OK;
+    });
+}
+
+dp_status dp_batch_remove(dp_batch *b, uint64_t id) {
+    return guarded([&] {
+        if (!b) throw Error(DP_ERR_INVALID, "null handle");
+        auto it = b->entries.find(id);
+        if (it == b->entries.end()) throw Error(DP_ERR_RANGE, "no such scene in the batch");
+        b->bind();
+        b->wait(kTimeoutMs); // the arena block may still be read by the last chunk
+        b->arena.release(it->second.offset, it->second.bytes);
+        b->slot_used[it->second.slot] = 0;
+        // Clear the slot's staged descriptor so a stale copy never runs.
+        for (int k = 0; k < 2; ++k) std::memset(&b->h_scenes[k][it->second.slot], 0, sizeof(BatchScene));
+        b->entries.erase(it);
+        b->dirty = true;
+        return DP_OK;
+    });
+}
+
+dp_status dp_batch_advance_chunk(dp_batch *b, uint32_t *stepping) {
+    return guarded([&] {
+        if (!b) throw Error(DP_ERR_INVALID, "null handle");
+        b->bind();
+        const uint32_t n = b->run_chunk();
+        if (stepping) *stepping = n;
+        return DP_OK;
+    });
+}
+
+dp_status dp_batch_wait(dp_batch *b, uint32_t timeout_ms) {
+    return guarded([&] {
+        if (!b) throw Error(DP_ERR_INVALID, "null handle");
+        b->bind();
+        b->wait(timeout_ms);
+        return DP_OK;
+    });
+}
+
+dp_status dp_batch_status(dp_batch *b, uint64_t id, uint64_t *step, uint64_t *target) {
+    return guarded([&] {
+        if (!b || !step || !target) throw Error(DP_ERR_INVALID, "null argument");
+        auto it = b->entries.find(id);
+        if (it == b->entries.end()) throw Error(DP_ERR_RANGE, "no such scene in the batch");
+        *step = it->second.step;
+        *target = it->second.target;
+        return DP_OK;
+    });
+}
+
+dp_status dp_batch_read_field(dp_batch *b, uint64_t id, uint32_t field, float *host, size_t count) {
+    return guarded([&] {
+        if (!b || !host) throw Error(DP_ERR_INVALID, "null argument");
+        auto it = b->entries.find(id);
+        if (it == b->entries.end()) throw Error(DP_ERR_RANGE, "no such scene in the batch");
+        const Entry &e = it->second;
+        const uint32_t *n = e.scene.grid.n;
+        const uint64_t cells = uint64_t(n[0]) * n[1] * n[2];
+        const int components = field == DP_FIELD_INTENSITY ? 1 : 3;
+        if (count != components * cells) throw Error(DP_ERR_RANGE, "element count does not match the field");
+        if (field == DP_FIELD_INTENSITY && !e.desc.intensity) throw Error(DP_ERR_INVALID, "intensity is not accumulated");
+        b->bind();
+        b->wait(kTimeoutMs);
+        const uint32_t current = uint32_t(e.step & 1u);
+        const float *src = field == DP_FIELD_ELECTRIC ? e.desc.e[current]
+                           : field == DP_FIELD_MAGNETIC ? e.desc.h[current] : e.desc.intensity;
+        if (field > DP_FIELD_INTENSITY) throw Error(DP_ERR_INVALID, "unknown field");
+        for (int c = 0; c < components; ++c)
+            check(cudaMemcpy2DAsync(host + c * cells, size_t(n[0]) * 4, src + c * e.cells_padded, size_t(e.pitch) * 4,
+                                    size_t(n[0]) * 4, size_t(n[1]) * n[2], cudaMemcpyDeviceToHost, b->stream),
+                  "readback");
+        b->wait(kTimeoutMs);
+        return DP_OK;
+    });
+}
+
+dp_status dp_batch_read_probes(dp_batch *b, uint64_t id, float *host, size_t count) {
+    return guarded([&] {
+        if (!b || !host) throw Error(DP_ERR_INVALID, "null argument");
+        auto it = b->entries.find(id);
+        if (it == b->entries.end()) throw Error(DP_ERR_RANGE, "no such scene in the batch");
+        const Entry &e = it->second;
+        const size_t n = size_t(e.step) * e.probe_cells.size() * 2;
+        if (count > n) throw Error(DP_ERR_RANGE, "more probe values than steps taken");
+        b->bind();
+        b->wait(kTimeoutMs);
+        if (count) check(cudaMemcpy(host, e.probes, count * sizeof(float), cudaMemcpyDeviceToHost), "probes");
+        return DP_OK;
+    });
+}
+
+dp_status dp_batch_memory(const dp_batch *b, uint64_t *used, uint64_t *capacity) {
+    return guarded([&] {
+        if (!b || !used || !capacity) throw Error(DP_ERR_INVALID, "null argument");
+        *used = b->arena.used();
+        *capacity = b->arena.capacity();
+        return DP_OK;
+    });
+}
+
+uint64_t dp_scene_batch_bytes(const dp_scene *scene, uint32_t probe_count, uint64_t steps) {
+    return scene ? layout_of(scene_of(scene), probe_count, steps).total : 0;
+}
+
+uint64_t dp_batch_launch_count(const dp_batch *b) { return b ? b->launches : 0; }
+
+} // extern "C"

@@ -15,7 +15,8 @@ namespace diaphane {
 // Tables a step kernel reads.  All pointers are device pointers.
 struct DeviceScene {
     uint32_t n[3];
-    uint64_t cells;
+    uint32_t pitch;          // row stride in cells (nx, or nx rounded up to 4 in a batch arena)
+    uint64_t cells;          // component stride: pitch * ny * nz
     const uint8_t *material; // cells
     const float4 *coeff;     // (electric_gain, electric_loss, magnetic_gain, magnetic_loss)
     const float *mgain;      // nx | ny | nz, c*dt/primary width
@@ -88,5 +89,44 @@ void fused_maps(const DeviceScene &s, const FusedPlan &plan, FieldSet set, const
                 uint32_t material_pitch, FusedMaps &out);
 void launch_fused_step(const DeviceScene &s, const FusedPlan &plan, const FusedMaps &in_maps, FieldSet out,
                        float *intensity, const InjectionTable &table, int32_t *error, cudaStream_t stream);
+
+// ---- batched form ------------------------------------------------------------
+
+// Injections per scene per step in a batch (2 slots per source).
+constexpr int kBatchInjections = 8;
+
+// One scene of a batch, in global memory.  The three 128-byte CUtensorMap
+// images come first so they keep the 64-byte alignment TMA requires.
+struct alignas(64) BatchScene {
+    unsigned char e_map[2][128];  // reading set 0 / set 1
+    unsigned char h_map[2][128];
+    unsigned char m_map[128];
+    DeviceScene s;
+    float *e[2];
+    float *h[2];
+    float *intensity;             // null: not accumulating
+    uint32_t parity;              // set that holds the fields at the chunk's first step
+    uint32_t steps;               // steps this scene takes in the chunk (0: idle)
+    uint64_t step0;               // the scene's step count at the chunk's first step
+};
+
+// One CTA's work: a tile of one scene through planes [z0, z1).
+struct BatchUnit {
+    uint32_t scene, x0, y0, z0, z1;
+};
+
+// Tensor maps of one batch scene (fields and index with row pitches).
+void batch_scene_maps(BatchScene &scene, uint32_t cx, uint32_t tile_y, const uint8_t *material,
+                      uint32_t material_pitch);
+// One launch per step over every unit of one kernel variant.
+void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, const BatchScene *scenes,
+                       const BatchUnit *units, uint32_t unit_count, const DeviceInjection *injections,
+                       const uint32_t *injection_counts, uint32_t scene_count, uint32_t step, int32_t *error,
+                       cudaStream_t stream);
+size_t fused_variant_smem(uint32_t cx, uint32_t tile_y, uint32_t slots);
+// Sets every batch kernel's shared-memory attributes (before any capture).
+void configure_batch_kernels();
+// Whether tensor maps can be encoded at all (driver entry point present).
+bool tensor_maps_available();
 
 } // namespace diaphane

@@ -177,6 +177,17 @@ template <int CX> __device__ __forceinline__ void stg(float *p, const Vec<CX> &r
     else __stcs(p, r.v[0]);
 }
 
+// Stores CX cells, or only the first `valid` of them at the end of a row.
+template <int CX> __device__ __forceinline__ void stg_row(float *p, const Vec<CX> &r, int valid) {
+    if (valid >= CX) {
+        stg<CX>(p, r);
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < CX; ++j)
+        if (j < valid) __stcs(p + j, r.v[j]);
+}
+
 // Profile or gain samples for CX consecutive cells along x; cells past the
 // end of the axis read as zero (they are never stored).  Scalar loads: the
 // sections of the packed tables need not be 16-byte aligned, and this runs
@@ -206,7 +217,14 @@ __device__ __forceinline__ float e_full(float e, float loss, float gain, float c
 // Bit k is set when injection k of `magnetic` phase covers row y and any of
 // the cells [xa, xb).  Computed once per thread; the per-plane test is then a
 // single z comparison per set bit.
-__device__ __forceinline__ uint32_t injection_mask(const InjectionTable &t, bool magnetic, int xa, int xb, int y) {
+// The injections of one step as the kernel reads them: a table in kernel
+// parameters (one scene) or in global memory (a batch).
+struct InjectionView {
+    const DeviceInjection *item;
+    uint32_t count;
+};
+
+__device__ __forceinline__ uint32_t injection_mask(const InjectionView &t, bool magnetic, int xa, int xb, int y) {
     uint32_t m = 0;
     for (uint32_t k = 0; k < t.count; ++k) {
         const DeviceInjection &d = t.item[k];
@@ -220,7 +238,7 @@ __device__ __forceinline__ uint32_t injection_mask(const InjectionTable &t, bool
 // Adds the injections in `mask` to the CX cells starting at x, in table
 // order — the reference's order (src/cpu.rs:606-633).
 template <int CX>
-__device__ __forceinline__ void apply_injections(const InjectionTable &t, const float *weights, uint32_t mask, int x,
+__device__ __forceinline__ void apply_injections(const InjectionView &t, const float *weights, uint32_t mask, int x,
                                                  int y, int z, Vec<CX> &f0, Vec<CX> &f1, Vec<CX> &f2) {
     while (mask) {
         const int k = __ffs(mask) - 1;
@@ -244,7 +262,7 @@ __device__ __forceinline__ void apply_injections(const InjectionTable &t, const 
     }
 }
 
-__device__ __forceinline__ void apply_injections_1(const InjectionTable &t, const float *weights, uint32_t mask,
+__device__ __forceinline__ void apply_injections_1(const InjectionView &t, const float *weights, uint32_t mask,
                                                    int x, int y, int z, float &f0, float &f1, float &f2) {
     Vec<1> a{{f0}}, b{{f1}}, c{{f2}};
     apply_injections<1>(t, weights, mask, x, y, z, a, b, c);
@@ -277,27 +295,33 @@ struct HaloCell {
     int x, y;
 };
 
-// Sixteen resident warps x 128 registers fill each SM sub-partition's
-// 16K-register file exactly: two CTAs of 8 warps, or one of 16.
+// What one CTA needs to advance one tile of one scene through a chunk of
+// z-planes.
+struct UnitArgs {
+    DeviceScene s;
+    float *e_out;
+    float *h_out;
+    float *intensity;       // null: not accumulating
+    int32_t *error;         // set when a wait gives up
+    InjectionView inj;
+    int x0, y0, z0, z1;     // tile origin and planes [z0, z1)
+};
+
+// The fused step for one (scene, tile, z-chunk) unit; every kernel below is
+// this function applied to a unit chosen from its block index.
 template <int CX, int TY, int SLOTS>
-__global__ void __launch_bounds__(32 * TY, 16 / TY)
-fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CUtensorMap h_map,
-           const __grid_constant__ CUtensorMap m_map, const __grid_constant__ FusedArgs args) {
+__device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUtensorMap *h_map_p,
+                                          const CUtensorMap *m_map_p, const UnitArgs &u) {
     using G = Geometry<CX, TY, SLOTS>;
     constexpr int kTileY = G::kTileY, kWarps = G::kWarps, kThreads = G::kThreads, kSlots = G::kSlots;
     extern __shared__ __align__(128) unsigned char smem[];
-    const DeviceScene &s = args.s;
-    const InjectionTable &inj = args.inj;
-    const int nx = int(s.n[0]), ny = int(s.n[1]), nz = int(s.n[2]);
+    const DeviceScene &s = u.s;
+    const InjectionView &inj = u.inj;
+    const int nx = int(s.n[0]), ny = int(s.n[1]);
+    const uint64_t pitch = s.pitch;
     const uint64_t cells = s.cells;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-    const uint32_t tile = blockIdx.x % (args.tiles_x * args.tiles_y);
-    const uint32_t chunk = blockIdx.x / (args.tiles_x * args.tiles_y);
-    const int x0 = int(tile % args.tiles_x) * G::TX;
-    const int y0 = int(tile / args.tiles_x) * kTileY;
-    const int z0 = int(chunk * args.z_chunk);
-    const int z1 = min(z0 + int(args.z_chunk), nz);
+    const int x0 = u.x0, y0 = u.y0, z0 = u.z0, z1 = u.z1;
     // A chunk that does not start at the bottom first rebuilds new H one
     // plane below itself: E(z0) needs it.
     const int zs = z0 > 0 ? z0 - 1 : z0;
@@ -319,9 +343,9 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
         unsigned char *slot = smem + k * G::SLOT;
         const uint32_t bar = bar0 + 8 * k;
         mbar_expect_tx(bar, G::TX_BYTES);
-        tma_load_4d(smem_addr(slot + G::E_OFF), &e_map, x0 - 4, y0 - 1, p, 0, bar);
-        tma_load_4d(smem_addr(slot + G::H_OFF), &h_map, x0 - 4, y0 - 1, p, 0, bar);
-        tma_load_3d(smem_addr(slot + G::M_OFF), &m_map, x0 - 16, y0 - 1, p, bar);
+        tma_load_4d(smem_addr(slot + G::E_OFF), e_map_p, x0 - 4, y0 - 1, p, 0, bar);
+        tma_load_4d(smem_addr(slot + G::H_OFF), h_map_p, x0 - 4, y0 - 1, p, 0, bar);
+        tma_load_3d(smem_addr(slot + G::M_OFF), m_map_p, x0 - 16, y0 - 1, p, bar);
     };
     const int last_plane = z1; // E(z1) feeds H(z1-1); past nz it arrives as zeros
     if (threadIdx.x == 0)
@@ -341,6 +365,9 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
     const float mgy = ldg_at(s.mgain + nx, y, ny), egy = ldg_at(s.egain + nx, y, ny);
     const float aiy = ldg_at(absorb_int + nx, y, ny), ahy = ldg_at(absorb_half + nx, y, ny);
     const bool store_row = y < ny && xl < nx;
+    // Cells at or past nx in this lane (only when the row pitch is wider than
+    // the grid) are computed but never stored.
+    const int full_lane = nx - xl >= CX ? CX : nx - xl;
     const bool has_inj = inj.count != 0;
     const uint32_t mask_h = has_inj ? injection_mask(inj, true, xl, xl + CX, y) : 0u;
     const uint32_t mask_e = has_inj ? injection_mask(inj, false, xl, xl + CX, y) : 0u;
@@ -389,7 +416,7 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
             // Give up on this chunk: report, then let the loads already in
             // flight land before the CTA's shared memory goes away.
             if (threadIdx.x == 0) {
-                atomicExch(args.error, 1);
+                atomicExch(u.error, 1);
                 for (int q = p; q <= min(p + kSlots - 1, last_plane); ++q) {
                     const int kq = (q - zs) % kSlots;
                     mbar_wait_bounded(bar0 + 8 * kq, uint32_t((q - zs) / kSlots) & 1u, kWaitCycles);
@@ -414,12 +441,12 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
         const bool prologue = p < z0;
         const float mgz = __ldg(&s.mgain[nx + ny + p]), egz = __ldg(&s.egain[nx + ny + p]);
         const float aiz = __ldg(&absorb_int[nx + ny + p]), ahz = __ldg(&absorb_half[nx + ny + p]);
-        const uint64_t at = uint64_t(p) * ny * nx + uint64_t(y) * nx + xl; // this lane's first cell
+        const uint64_t at = (uint64_t(p) * ny + uint64_t(y)) * pitch + xl; // this lane's first cell
 
         // Intensity of this thread's cells, fetched early.
         Vec<CX> inten;
-        const bool accumulate = args.intensity != nullptr && !prologue && store_row;
-        if (accumulate) inten = ldg<CX>(args.intensity + at);
+        const bool accumulate = u.intensity != nullptr && !prologue && store_row;
+        if (accumulate) inten = ldg<CX>(u.intensity + at);
 
         // Material coefficients of this lane's cells, kept for the E phase.
         float2 ecoef[CX]; // (electric_gain, electric_loss)
@@ -510,9 +537,9 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
                 sts<CX>(h_at(H, 1, row, col), nhy);
                 sts<CX>(h_at(H, 2, row, col), nhz);
                 if (store_row) {
-                    stg<CX>(args.h_out + at, nhx);
-                    stg<CX>(args.h_out + cells + at, nhy);
-                    stg<CX>(args.h_out + 2 * cells + at, nhz);
+                    stg_row<CX>(u.h_out + at, nhx, full_lane);
+                    stg_row<CX>(u.h_out + cells + at, nhy, full_lane);
+                    stg_row<CX>(u.h_out + 2 * cells + at, nhz, full_lane);
                 }
             }
         }
@@ -620,9 +647,9 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
             }
             if (mask_e) apply_injections<CX>(inj, s.weights, mask_e, xl, y, p, ex, ey, ez);
             if (store_row) {
-                stg<CX>(args.e_out + at, ex);
-                stg<CX>(args.e_out + cells + at, ey);
-                stg<CX>(args.e_out + 2 * cells + at, ez);
+                stg_row<CX>(u.e_out + at, ex, full_lane);
+                stg_row<CX>(u.e_out + cells + at, ey, full_lane);
+                stg_row<CX>(u.e_out + 2 * cells + at, ez, full_lane);
                 if (accumulate) {
 #pragma unroll
                     for (int j = 0; j < CX; ++j) {
@@ -631,7 +658,7 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
                         sum += ez.v[j] * ez.v[j];
                         inten.v[j] += sum;
                     }
-                    stg<CX>(args.intensity + at, inten);
+                    stg_row<CX>(u.intensity + at, inten, full_lane);
                 }
             }
             hx_prev = hx;
@@ -640,6 +667,65 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
     }
     // Every issued plane has been waited for (the loop waits through plane
     // z1, the last one issued), so no copy is still landing here.
+}
+
+// One scene: block b is tile b % tiles of z-chunk b / tiles.  Sixteen
+// resident warps x 128 registers fill each SM sub-partition's 16K-register
+// file exactly: two CTAs of 8 warps, or one of 16.
+template <int CX, int TY, int SLOTS>
+__global__ void __launch_bounds__(32 * TY, 16 / TY)
+fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CUtensorMap h_map,
+           const __grid_constant__ CUtensorMap m_map, const __grid_constant__ FusedArgs args) {
+    const uint32_t tiles = args.tiles_x * args.tiles_y;
+    const uint32_t tile = blockIdx.x % tiles, chunk = blockIdx.x / tiles;
+    UnitArgs u;
+    u.s = args.s;
+    u.e_out = args.e_out;
+    u.h_out = args.h_out;
+    u.intensity = args.intensity;
+    u.error = args.error;
+    u.inj = InjectionView{args.inj.item, args.inj.count};
+    u.x0 = int(tile % args.tiles_x) * 32 * CX;
+    u.y0 = int(tile / args.tiles_x) * TY;
+    u.z0 = int(chunk * args.z_chunk);
+    u.z1 = min(u.z0 + int(args.z_chunk), int(args.s.n[2]));
+    step_unit<CX, TY, SLOTS>(&e_map, &h_map, &m_map, u);
+}
+
+// A batch: block b is unit b of this variant's work list.  Scene descriptors
+// (with their tensor maps) live in global memory; a scene that has finished
+// its steps for this chunk, or has left the batch, is skipped.
+template <int CX, int TY, int SLOTS>
+__global__ void __launch_bounds__(32 * TY, 16 / TY)
+fused_batch_step(const BatchScene *__restrict__ scenes, const BatchUnit *__restrict__ units,
+                 const DeviceInjection *__restrict__ injections, const uint32_t *__restrict__ injection_counts,
+                 uint32_t scene_count, uint32_t step, int32_t *error) {
+    const BatchUnit unit = units[blockIdx.x];
+    const BatchScene &bs = scenes[unit.scene];
+    if (step >= bs.steps) return;
+    const uint32_t p = (bs.parity + step) & 1u;
+    const CUtensorMap *e_map = reinterpret_cast<const CUtensorMap *>(bs.e_map[p]);
+    const CUtensorMap *h_map = reinterpret_cast<const CUtensorMap *>(bs.h_map[p]);
+    const CUtensorMap *m_map = reinterpret_cast<const CUtensorMap *>(bs.m_map);
+    if (threadIdx.x == 0) {
+        // The descriptors were written by a host copy since the last launch.
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(e_map) : "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(h_map) : "memory");
+        asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(m_map) : "memory");
+    }
+    UnitArgs u;
+    u.s = bs.s;
+    u.e_out = bs.e[p ^ 1u];
+    u.h_out = bs.h[p ^ 1u];
+    u.intensity = bs.intensity;
+    u.error = error;
+    const size_t slot = size_t(step) * scene_count + unit.scene;
+    u.inj = InjectionView{injections + slot * kBatchInjections, injection_counts[slot]};
+    u.x0 = int(unit.x0);
+    u.y0 = int(unit.y0);
+    u.z0 = int(unit.z0);
+    u.z1 = int(unit.z1);
+    step_unit<CX, TY, SLOTS>(e_map, h_map, m_map, u);
 }
 
 // ---- host side ----------------------------------------------------------------
@@ -764,25 +850,89 @@ FusedPlan fused_plan(const uint32_t n[3], uint32_t cx, uint32_t tile_y, uint32_t
     return p;
 }
 
+namespace {
+
+// Field maps: the grid's true extent with the arena's row pitch, so reads past
+// nx arrive as zeros (the wall) whatever the padding holds.
+void encode_field_maps(const DeviceScene &s, uint32_t tx, uint32_t ty, float *e, float *h, void *e_out,
+                       void *h_out) {
+    const cuuint64_t nx = s.n[0], ny = s.n[1], nz = s.n[2], pitch = s.pitch;
+    cuuint64_t dims[4] = {nx, ny, nz, 3};
+    cuuint64_t strides[3] = {pitch * 4, pitch * ny * 4, pitch * ny * nz * 4};
+    cuuint32_t ebox[4] = {tx + 8, ty + 2, 1, 3};
+    cuuint32_t hbox[4] = {tx + 8, ty + 1, 1, 3};
+    encode(reinterpret_cast<CUtensorMap *>(e_out), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, e, dims, strides, ebox);
+    encode(reinterpret_cast<CUtensorMap *>(h_out), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, h, dims, strides, hbox);
+}
+
+void encode_index_map(const DeviceScene &s, uint32_t tx, uint32_t ty, const uint8_t *material,
+                      uint32_t material_pitch, void *out) {
+    const cuuint64_t ny = s.n[1], nz = s.n[2];
+    cuuint64_t dims[3] = {material_pitch, ny, nz};
+    cuuint64_t strides[2] = {material_pitch, cuuint64_t(material_pitch) * ny};
+    cuuint32_t box[3] = {tx + 32, ty + 1, 1};
+    encode(reinterpret_cast<CUtensorMap *>(out), CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<uint8_t *>(material),
+           dims, strides, box);
+}
+
+} // namespace
+
 void fused_maps(const DeviceScene &s, const FusedPlan &plan, FieldSet set, const uint8_t *material_padded,
                 uint32_t material_pitch, FusedMaps &out) {
     const uint32_t tx = 32u * plan.cx, ty = plan.tile_y;
-    const cuuint64_t nx = s.n[0], ny = s.n[1], nz = s.n[2];
-    {
-        cuuint64_t dims[4] = {nx, ny, nz, 3};
-        cuuint64_t strides[3] = {nx * 4, nx * ny * 4, nx * ny * nz * 4};
-        cuuint32_t ebox[4] = {tx + 8, ty + 2, 1, 3};
-        cuuint32_t hbox[4] = {tx + 8, ty + 1, 1, 3};
-        encode(reinterpret_cast<CUtensorMap *>(out.e), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, set.e, dims, strides, ebox);
-        encode(reinterpret_cast<CUtensorMap *>(out.h), CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, set.h, dims, strides, hbox);
-    }
-    {
-        cuuint64_t dims[3] = {material_pitch, ny, nz};
-        cuuint64_t strides[2] = {material_pitch, cuuint64_t(material_pitch) * ny};
-        cuuint32_t box[3] = {tx + 32, ty + 1, 1};
-        encode(reinterpret_cast<CUtensorMap *>(out.m), CU_TENSOR_MAP_DATA_TYPE_UINT8, 3,
-               const_cast<uint8_t *>(material_padded), dims, strides, box);
-    }
+    encode_field_maps(s, tx, ty, set.e, set.h, out.e, out.h);
+    encode_index_map(s, tx, ty, material_padded, material_pitch, out.m);
+}
+
+void batch_scene_maps(BatchScene &scene, uint32_t cx, uint32_t tile_y, const uint8_t *material,
+                      uint32_t material_pitch) {
+    const uint32_t tx = 32u * cx;
+    for (int k = 0; k < 2; ++k) encode_field_maps(scene.s, tx, tile_y, scene.e[k], scene.h[k], scene.e_map[k], scene.h_map[k]);
+    encode_index_map(scene.s, tx, tile_y, material, material_pitch, scene.m_map);
+}
+
+size_t fused_variant_smem(uint32_t cx, uint32_t tile_y, uint32_t slots) { return variant_smem(cx, tile_y, slots); }
+
+namespace {
+
+template <int CX, int TY, int SLOTS> void configure_batch_variant() {
+    cudaFuncSetAttribute(fused_batch_step<CX, TY, SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         Geometry<CX, TY, SLOTS>::SMEM);
+    cudaFuncSetAttribute(fused_batch_step<CX, TY, SLOTS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+}
+
+template <int CX, int TY, int SLOTS>
+void launch_batch_variant(const BatchScene *scenes, const BatchUnit *units, uint32_t unit_count,
+                          const DeviceInjection *injections, const uint32_t *counts, uint32_t scene_count,
+                          uint32_t step, int32_t *error, cudaStream_t stream) {
+    fused_batch_step<CX, TY, SLOTS><<<unit_count, 32 * TY, Geometry<CX, TY, SLOTS>::SMEM, stream>>>(
+        scenes, units, injections, counts, scene_count, step, error);
+}
+
+} // namespace
+
+void configure_batch_kernels() {
+    configure_batch_variant<4, 8, 3>();
+    configure_batch_variant<2, 8, 5>();
+    configure_batch_variant<4, 16, 3>();
+    configure_batch_variant<1, 8, 5>();
+}
+
+bool tensor_maps_available() { return encoder() != nullptr; }
+
+void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, const BatchScene *scenes,
+                       const BatchUnit *units, uint32_t unit_count, const DeviceInjection *injections,
+                       const uint32_t *injection_counts, uint32_t scene_count, uint32_t step, int32_t *error,
+                       cudaStream_t stream) {
+    if (unit_count == 0) return;
+    if (cx == 4 && tile_y == 8 && slots == 3)
+        launch_batch_variant<4, 8, 3>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
+    else if (cx == 2 && tile_y == 8 && slots == 5)
+        launch_batch_variant<2, 8, 5>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
+    else if (cx == 4 && tile_y == 16 && slots == 3)
+        launch_batch_variant<4, 16, 3>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
+    else
+        launch_batch_variant<1, 8, 5>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
 }
 
 void launch_fused_step(const DeviceScene &s, const FusedPlan &plan, const FusedMaps &in_maps, FieldSet out,

@@ -220,6 +220,7 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
 
     DeviceScene &d = sim->dev;
     for (int a = 0; a < 3; ++a) d.n[a] = s.grid.n[a];
+    d.pitch = s.grid.n[0];
     d.cells = cells;
     d.material = device_upload(s.material_index, owned, st);
     // Padded to all 256 u8 indices, so a kernel may stage the whole table.

@@ -125,3 +125,39 @@ def graded_stack(open_boundary: bool = True) -> Scene:
     f0 = 299792458.0 / lam0
     scene.sources.append(Source.sheet(Axis.X, -0.15, 0.06, Axis.Z, Waveform.gaussian_pulse(f0, 3.0)))
     return scene
+
+
+def mixed_scene(seed: int, lo: int = 32, hi: int = 160, steps: int = 1000) -> Scene:
+    """One scene of the mixed-size batch: each axis log-uniform in [lo, hi]
+    cells at 1 mm, 10-cell absorber, up to 8 seeded dielectric spheres (εr in
+    [1, 4]), a perfectly conducting sphere with probability 1/2, and one
+    source — a point dipole or, with probability 1/2, an x-travelling plane
+    wave — at 10 cells per wavelength."""
+    rng = SplitMix64(seed)
+    n = [int(round(math.exp(rng.uniform(math.log(lo), math.log(hi))))) for _ in range(3)]
+    cell = f32(1e-3)
+    scene = Scene.empty(Extent(*n), float(cell))
+    half = [f32(v) * cell / f32(2.0) for v in n]
+    margin = 12  # clear of the absorber (and of the plane-wave rows)
+
+    def inside(axis: int, radius: float) -> float:
+        lo_c, hi_c = margin + radius, n[axis] - margin - radius
+        c = rng.uniform(lo_c, hi_c) if hi_c > lo_c else n[axis] / 2.0
+        return float(f32(c) * cell - half[axis])
+
+    for _ in range(int(rng.uniform(0, 9))):
+        r = rng.uniform(2.0, max(2.5, min(n) / 8.0))
+        m = scene.materials.push(Material.dielectric(rng.uniform(1.0, 4.0)))
+        scene.shapes.append(Shape.sphere((inside(0, r + 16), inside(1, r), inside(2, r)), float(f32(r) * cell), m))
+    if rng.uniform(0, 1) < 0.5:
+        r = max(2.0, min(n) / 10.0)
+        pec = scene.materials.push(Material.PERFECT_CONDUCTOR)
+        scene.shapes.append(Shape.sphere((inside(0, r + 16), inside(1, r), inside(2, r)), float(f32(r) * cell), pec))
+    frequency = scene.grid.frequency_for_resolution(10.0)
+    if rng.uniform(0, 1) < 0.5:
+        scene.sources.append(Source.point((inside(0, 4), inside(1, 4), inside(2, 4)), Axis.Z,
+                                          Waveform.gaussian_pulse(frequency, 3.0)))
+    else:
+        scene.sources.append(Source.plane_wave(Axis.X, float(f32(13.5) * cell - half[0]), Axis.Z,
+                                               Waveform.gaussian_pulse(frequency, 3.0)))
+    return scene

@@ -289,6 +289,48 @@ dp_status dp_sim_energy(dp_sim *sim, double *electric, double *magnetic);
 dp_status dp_sim_is_finite(dp_sim *sim, int32_t *finite);
 /* is_reversible (src/cpu.rs:209-215). */
 int32_t dp_sim_is_reversible(const dp_sim *sim);
+/* ------------------------------------------------------------------------ */
+/* Batched form: many scenes of uneven sizes advanced together              */
+/* ------------------------------------------------------------------------ */
+/* No single counterpart in the reference, which runs one scene per
+ * gpu::Simulation: a batch is many Simulation::advance_by calls
+ * (src/gpu.rs:393-484) merged into one launch per step over a work list of
+ * (scene, tile, z-chunk) units, with K-step chunks replayed as CUDA graphs.
+ * Each scene's results are bit-identical to its solo run. */
+
+typedef struct dp_batch dp_batch;
+
+typedef struct dp_batch_options {
+    int32_t device;
+    uint32_t chunk_steps; /* steps per graph replay (K); 0 = 50 */
+    uint64_t arena_bytes; /* device memory for every scene's state */
+    uint32_t max_scenes;  /* scene slots; 0 = 256 */
+    uint32_t use_graphs;  /* 0: launch each chunk's kernels directly */
+} dp_batch_options;
+
+dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out);
+void dp_batch_destroy(dp_batch *batch);
+/* Admits a scene for `steps` steps, or DP_ERR_OOM when the arena cannot hold
+ * it now, DP_ERR_BUSY when every slot is taken.  probes: probe_count
+ * (x, y, z) cells whose Ez and Hy are recorded after every step.  Takes
+ * effect at the next chunk. */
+dp_status dp_batch_add(dp_batch *batch, const dp_scene *scene, uint64_t steps, int32_t accumulate_intensity,
+                       const uint32_t *probes, uint32_t probe_count, uint64_t *id);
+/* Frees a scene's slot and arena block (waits for the running chunk). */
+dp_status dp_batch_remove(dp_batch *batch, uint64_t id);
+/* One chunk for every scene with steps left (asynchronous). */
+dp_status dp_batch_advance_chunk(dp_batch *batch, uint32_t *stepping);
+dp_status dp_batch_wait(dp_batch *batch, uint32_t timeout_ms);
+dp_status dp_batch_status(dp_batch *batch, uint64_t id, uint64_t *step, uint64_t *target);
+/* read_electric / read_magnetic / read_intensity of one scene, dense. */
+dp_status dp_batch_read_field(dp_batch *batch, uint64_t id, uint32_t field, float *host, size_t count);
+/* Probe series: step-major, then probe, then (Ez, Hy). */
+dp_status dp_batch_read_probes(dp_batch *batch, uint64_t id, float *host, size_t count);
+dp_status dp_batch_memory(const dp_batch *batch, uint64_t *used, uint64_t *capacity);
+/* Arena bytes a scene would take (for admission control). */
+uint64_t dp_scene_batch_bytes(const dp_scene *scene, uint32_t probe_count, uint64_t steps);
+uint64_t dp_batch_launch_count(const dp_batch *batch);
+
 /* Field energy of caller-owned device arrays, allocating nothing.  No
  * counterpart in the reference: it exists for callers that cannot call
  * cudaMalloc where they need the energy (cudaMalloc may synchronize the

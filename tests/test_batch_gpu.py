@@ -1,0 +1,101 @@
+"""The batched form: every scene of a mixed batch must come out bit-identical
+to its own solo run (and so to the oracle), whatever else shares the launch,
+however the work is chunked, and whenever it joined."""
+import numpy as np
+import pytest
+
+import oracle
+from diaphane_gb300 import Batch, DP_KERNEL_NAIVE, ResolvedScene, Simulation, workloads
+from tests import scenes
+
+pytestmark = pytest.mark.gpu
+
+ARENA = 4 << 30
+
+
+def bits(a):
+    return a.view(np.uint32)
+
+
+def mixed(count, steps, seed0=1000, hi=72):
+    return [ResolvedScene(workloads.mixed_scene(seed0 + k, lo=24, hi=hi)) for k in range(count)]
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_a_mixed_batch_matches_each_scene_run_alone(graphs):
+    resolved = mixed(12, 120)
+    batch = Batch(ARENA, chunk_steps=16, max_scenes=16, use_graphs=graphs)
+    ids = [batch.add(r, 120 - 7 * k, accumulate_intensity=(k % 2 == 0)) for k, r in enumerate(resolved)]
+    batch.run_to_completion()
+    for k, (ident, r) in enumerate(zip(ids, resolved)):
+        solo = Simulation(r, kernel=DP_KERNEL_NAIVE)
+        solo.set_accumulate_intensity(k % 2 == 0)
+        solo.advance_by(120 - 7 * k)
+        assert batch.status(ident) == (120 - 7 * k, 120 - 7 * k)
+        assert np.array_equal(bits(batch.read_electric(ident)), bits(solo.read_electric())), k
+        assert np.array_equal(bits(batch.read_magnetic(ident)), bits(solo.read_magnetic())), k
+        if k % 2 == 0:
+            assert np.array_equal(bits(batch.read_intensity(ident)), bits(solo.read_intensity())), k
+
+
+def test_scenes_that_join_and_leave_between_chunks(threads):
+    """Continuous batching: a newcomer joins a running batch; results are the
+    same as alone (checked against the oracle here)."""
+    first, second = mixed(2, 0, seed0=2000)
+    batch = Batch(ARENA, chunk_steps=10, max_scenes=4)
+    a = batch.add(first, 95)
+    for _ in range(4):
+        batch.advance_chunk()
+    b = batch.add(second, 60)       # joins at step 40 of the first
+    batch.run_to_completion()
+    for ident, r, steps in ((a, first, 95), (b, second, 60)):
+        ref = oracle.OracleSimulation(r.scene, threads=threads)
+        ref.advance_by(steps)
+        assert np.array_equal(bits(batch.read_electric(ident)), bits(ref.read_electric()))
+        assert np.array_equal(bits(batch.read_magnetic(ident)), bits(ref.read_magnetic()))
+    batch.remove(a)
+    used, cap = batch.memory()
+    assert 0 < used < cap
+
+
+def test_the_parity_scenes_in_one_batch(threads):
+    cases = {name: make() for name, make in scenes.PARITY_CASES.items()}
+    batch = Batch(ARENA, chunk_steps=50, max_scenes=16)
+    ids = {name: batch.add(ResolvedScene(scene), steps) for name, (scene, steps) in cases.items()}
+    batch.run_to_completion()
+    for name, (scene, steps) in cases.items():
+        ref = oracle.OracleSimulation(scene, threads=threads)
+        ref.advance_by(steps)
+        assert np.array_equal(bits(batch.read_electric(ids[name])), bits(ref.read_electric())), name
+        assert np.array_equal(bits(batch.read_magnetic(ids[name])), bits(ref.read_magnetic())), name
+
+
+def test_probes_record_ez_and_hy_every_step():
+    (r,) = mixed(1, 0, seed0=3000)
+    probes = [(5, 6, 7), (r.extent[0] // 2, r.extent[1] // 2, r.extent[2] // 2)]
+    batch = Batch(ARENA, chunk_steps=8, max_scenes=2)
+    ident = batch.add(r, 30, probes=probes)
+    batch.run_to_completion()
+    series = batch.read_probes(ident)
+    assert series.shape == (30, 2, 2)
+    solo = Simulation(r, kernel=DP_KERNEL_NAIVE)
+    cells = r.cells
+    for step in range(1, 31):
+        solo.advance_by(1)
+        e, h = solo.read_electric(), solo.read_magnetic()
+        for k, (x, y, z) in enumerate(probes):
+            i = (z * r.extent[1] + y) * r.extent[0] + x
+            assert series[step - 1, k, 0] == e[2 * cells + i]
+            assert series[step - 1, k, 1] == h[cells + i]
+
+
+def test_admission_refuses_what_the_arena_cannot_hold():
+    (r,) = mixed(1, 0, seed0=4000, hi=48)
+    need = Batch.bytes_for(r, 100)
+    batch = Batch(int(need * 2.5), chunk_steps=10, max_scenes=8)
+    batch.add(r, 100)
+    batch.add(r, 100)
+    from diaphane_gb300 import DiaphaneError
+    with pytest.raises(DiaphaneError) as err:
+        batch.add(r, 100)
+    assert err.value.name == "DP_ERR_OOM"
