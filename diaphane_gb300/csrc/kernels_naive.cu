@@ -13,11 +13,14 @@ namespace {
 
 constexpr int kThreads = 256;
 
-__device__ __forceinline__ void decompose(uint64_t i, const uint32_t n[3], uint32_t c[3]) {
-    c[0] = uint32_t(i % n[0]);
-    uint64_t t = i / n[0];
-    c[1] = uint32_t(t % n[1]);
-    c[2] = uint32_t(t / n[1]);
+// Cell coordinates of linear index i in a layout whose rows are `pitch`
+// cells long; false for the padding cells past nx.
+__device__ __forceinline__ bool decompose(uint64_t i, const DeviceScene &s, uint32_t c[3]) {
+    c[0] = uint32_t(i % s.pitch);
+    const uint64_t t = i / s.pitch;
+    c[1] = uint32_t(t % s.n[1]);
+    c[2] = uint32_t(t / s.n[1]);
+    return c[0] < s.n[0];
 }
 
 // Absorber sample: section 0 holds integer positions, section 1 half ones.
@@ -35,8 +38,8 @@ __global__ void __launch_bounds__(kThreads) magnetic_pass(DeviceScene s, const f
     const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
     if (i >= s.cells) return;
     uint32_t c[3];
-    decompose(i, s.n, c);
-    const uint64_t stride[3] = {1, s.n[0], uint64_t(s.n[0]) * s.n[1]};
+    if (!decompose(i, s, c)) return;
+    const uint64_t stride[3] = {1, s.pitch, uint64_t(s.pitch) * s.n[1]};
     const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
     const uint32_t span = s.n[0] + s.n[1] + s.n[2];
     const float4 k = s.coeff[s.material[i]];
@@ -70,8 +73,8 @@ __global__ void __launch_bounds__(kThreads) electric_pass(DeviceScene s, const f
     const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
     if (i >= s.cells) return;
     uint32_t c[3];
-    decompose(i, s.n, c);
-    const uint64_t stride[3] = {1, s.n[0], uint64_t(s.n[0]) * s.n[1]};
+    if (!decompose(i, s, c)) return;
+    const uint64_t stride[3] = {1, s.pitch, uint64_t(s.pitch) * s.n[1]};
     const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
     const uint32_t span = s.n[0] + s.n[1] + s.n[2];
     const float4 k = s.coeff[s.material[i]];
@@ -105,7 +108,7 @@ __global__ void __launch_bounds__(kThreads) inject_pass(DeviceScene s, FieldSet 
     const uint64_t t = i / inj.extent[0];
     const uint32_t dy = uint32_t(t % inj.extent[1]);
     const uint32_t dz = uint32_t(t / inj.extent[1]);
-    const uint64_t cell = (uint64_t(inj.origin[2] + dz) * s.n[1] + (inj.origin[1] + dy)) * s.n[0] + inj.origin[0] + dx;
+    const uint64_t cell = (uint64_t(inj.origin[2] + dz) * s.n[1] + (inj.origin[1] + dy)) * s.pitch + inj.origin[0] + dx;
     const float weight = inj.weight_offset < 0 ? 1.0f : __ldg(&s.weights[inj.weight_offset + i]);
     float *field = (inj.magnetic ? f.h : f.e) + uint64_t(inj.component) * s.cells;
     field[cell] += (sign * inj.value) * weight;
@@ -133,7 +136,7 @@ __global__ void __launch_bounds__(kThreads) energy_pass(DeviceScene s, FieldSet 
     for (uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x; i < s.cells;
          i += uint64_t(gridDim.x) * kThreads) {
         uint32_t c[3];
-        decompose(i, s.n, c);
+        if (!decompose(i, s, c)) continue;
         const float2 m = eps_mu[s.material[i]];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {

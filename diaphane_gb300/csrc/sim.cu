@@ -63,6 +63,7 @@ struct dp_sim {
     int32_t *error = nullptr;        // set by a kernel whose bounded wait gave up
     uint8_t *material_padded = nullptr;
     uint32_t material_pitch = 0;
+    uint32_t pitch = 0;              // field row stride in cells (nx rounded up to 4)
     FusedPlan plan{};
     FusedMaps maps[2]{};             // tensor maps reading set 0 / set 1
     std::vector<void *> owned;
@@ -166,10 +167,30 @@ struct dp_sim {
         }
     }
 
+    uint64_t padded_cells() const { return uint64_t(pitch) * scene.grid.n[1] * scene.grid.n[2]; }
+
     void clear_intensity() {
         if (accumulated == 0) return;
-        check(cudaMemsetAsync(intensity, 0, scene.grid.cells() * sizeof(float), stream), "clear intensity");
+        check(cudaMemsetAsync(intensity, 0, padded_cells() * sizeof(float), stream), "clear intensity");
         accumulated = 0;
+    }
+
+    // Dense host rows <-> pitched device rows, `components` of them.
+    void copy_out(float *host, const float *device, int components) {
+        const uint32_t *n = scene.grid.n;
+        const uint64_t dense = scene.grid.cells(), padded = padded_cells();
+        for (int c = 0; c < components; ++c)
+            check(cudaMemcpy2DAsync(host + c * dense, size_t(n[0]) * 4, device + c * padded, size_t(pitch) * 4,
+                                    size_t(n[0]) * 4, size_t(n[1]) * n[2], cudaMemcpyDeviceToHost, stream),
+                  "readback");
+    }
+    void copy_in(float *device, const float *host, int components) {
+        const uint32_t *n = scene.grid.n;
+        const uint64_t dense = scene.grid.cells(), padded = padded_cells();
+        for (int c = 0; c < components; ++c)
+            check(cudaMemcpy2DAsync(device + c * padded, size_t(pitch) * 4, host + c * dense, size_t(n[0]) * 4,
+                                    size_t(n[0]) * 4, size_t(n[1]) * n[2], cudaMemcpyHostToDevice, stream),
+                  "upload");
     }
 
     void wait(uint32_t timeout_ms) {
@@ -207,22 +228,33 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
     check(cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking), "cudaStreamCreate");
 
     const Scene &s = sim->scene;
-    const uint64_t cells = s.grid.cells();
+    // Rows are padded to a multiple of 4 cells (16 bytes) so the fused step's
+    // tensor maps can stride them; for such grids the layout is the
+    // reference's dense one exactly.
+    const uint32_t nx = s.grid.n[0];
+    sim->pitch = (nx + 3) / 4 * 4;
+    const uint64_t cells = uint64_t(sim->pitch) * s.grid.n[1] * s.grid.n[2];
     auto &owned = sim->owned;
     cudaStream_t st = sim->stream;
 
     uint32_t requested = opts ? opts->kernel : DP_KERNEL_AUTO;
     if (requested > DP_KERNEL_NAIVE) throw Error(DP_ERR_INVALID, "unknown kernel selector");
-    const bool fits = fused_supported(s.grid.n) && 2 * s.sources.size() <= size_t(kMaxInjections);
+    const bool fits = tensor_maps_available() && 2 * s.sources.size() <= size_t(kMaxInjections);
     if (requested == DP_KERNEL_FUSED && !fits)
         throw Error(DP_ERR_UNSUPPORTED, "the fused step does not cover this grid shape or source count");
     sim->kernel = (requested == DP_KERNEL_NAIVE || !fits) ? DP_KERNEL_NAIVE : DP_KERNEL_FUSED;
 
     DeviceScene &d = sim->dev;
     for (int a = 0; a < 3; ++a) d.n[a] = s.grid.n[a];
-    d.pitch = s.grid.n[0];
+    d.pitch = sim->pitch;
     d.cells = cells;
-    d.material = device_upload(s.material_index, owned, st);
+    {
+        std::vector<uint8_t> pitched(cells, 0);
+        const uint64_t rows = uint64_t(s.grid.n[1]) * s.grid.n[2];
+        for (uint64_t r = 0; r < rows; ++r)
+            std::memcpy(&pitched[r * sim->pitch], &s.material_index[r * nx], nx);
+        d.material = device_upload(pitched, owned, st);
+    }
     // Padded to all 256 u8 indices, so a kernel may stage the whole table.
     std::vector<float4> coeff(256, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     for (size_t m = 0; m < s.coefficients.size(); ++m) {
@@ -250,7 +282,7 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
     if (sets == 1) sim->set[1] = sim->set[0];
     sim->intensity = device_alloc<float>(cells, owned);
     check(cudaMemsetAsync(sim->intensity, 0, cells * sizeof(float), st), "memset");
-    const uint32_t blocks = energy_blocks(cells);
+    const uint32_t blocks = energy_blocks(cells);  // padded cells
     sim->partials = device_alloc<double>(2 * size_t(blocks), owned);
     check(cudaMallocHost(&sim->host_partials, 2 * size_t(blocks) * sizeof(double)), "cudaMallocHost");
     sim->flag = device_alloc<int32_t>(1, owned);
@@ -267,7 +299,7 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
             throw Error(DP_ERR_UNSUPPORTED, e.what());
         }
         // The index again with rows padded to 16 bytes, for its tensor map.
-        const uint32_t nx = s.grid.n[0], rows = s.grid.n[1] * s.grid.n[2];
+        const uint32_t rows = s.grid.n[1] * s.grid.n[2];
         sim->material_pitch = (nx + 15) / 16 * 16;
         std::vector<uint8_t> padded(size_t(sim->material_pitch) * rows, 0);
         for (size_t r = 0; r < rows; ++r)
@@ -342,7 +374,7 @@ dp_status dp_sim_reset(dp_sim *sim) {
     return guarded([&] {
         if (!sim) throw Error(DP_ERR_INVALID, "null handle");
         sim->bind();
-        const uint64_t cells = sim->scene.grid.cells();
+        const uint64_t cells = sim->padded_cells();
         for (int k = 0; k < 2; ++k) {
             check(cudaMemsetAsync(sim->set[k].e, 0, 3 * cells * sizeof(float), sim->stream), "reset");
             check(cudaMemsetAsync(sim->set[k].h, 0, 3 * cells * sizeof(float), sim->stream), "reset");
@@ -374,8 +406,7 @@ dp_status dp_sim_read_field(dp_sim *sim, uint32_t field, float *host, size_t cou
         if (count != field_count(sim, field)) throw Error(DP_ERR_RANGE, "element count does not match the field");
         sim->bind();
         sim->wait(kDefaultTimeoutMs);
-        check(cudaMemcpyAsync(host, field_ptr(sim, field), count * sizeof(float), cudaMemcpyDeviceToHost, sim->stream),
-              "readback");
+        sim->copy_out(host, field_ptr(sim, field), field == DP_FIELD_INTENSITY ? 1 : 3);
         sim->wait(kDefaultTimeoutMs);
         return DP_OK;
     });
@@ -387,8 +418,7 @@ dp_status dp_sim_write_field(dp_sim *sim, uint32_t field, const float *host, siz
         if (count != field_count(sim, field)) throw Error(DP_ERR_RANGE, "snapshot was taken from a different grid");
         sim->bind();
         sim->wait(kDefaultTimeoutMs);
-        check(cudaMemcpyAsync(field_ptr(sim, field), host, count * sizeof(float), cudaMemcpyHostToDevice, sim->stream),
-              "upload");
+        sim->copy_in(field_ptr(sim, field), host, field == DP_FIELD_INTENSITY ? 1 : 3);
         sim->wait(kDefaultTimeoutMs);
         return DP_OK;
     });
@@ -402,8 +432,8 @@ dp_status dp_sim_restore(dp_sim *sim, uint64_t step, const float *electric, cons
         // The average belongs to the history that was just abandoned.
         sim->clear_intensity();
         sim->wait(kDefaultTimeoutMs);
-        check(cudaMemcpyAsync(sim->fields().e, electric, count * sizeof(float), cudaMemcpyHostToDevice, sim->stream), "restore");
-        check(cudaMemcpyAsync(sim->fields().h, magnetic, count * sizeof(float), cudaMemcpyHostToDevice, sim->stream), "restore");
+        sim->copy_in(sim->fields().e, electric, 3);
+        sim->copy_in(sim->fields().h, magnetic, 3);
         sim->wait(kDefaultTimeoutMs);
         sim->step = step;
         return DP_OK;
@@ -446,7 +476,7 @@ dp_status dp_sim_energy(dp_sim *sim, double *electric, double *magnetic) {
     return guarded([&] {
         if (!sim || !electric || !magnetic) throw Error(DP_ERR_INVALID, "null argument");
         sim->bind();
-        const uint32_t blocks = energy_blocks(sim->scene.grid.cells());
+        const uint32_t blocks = energy_blocks(sim->padded_cells());
         launch_energy(sim->dev, sim->fields(), sim->primary, sim->dual, sim->eps_mu, sim->partials, blocks, sim->stream);
         ++sim->launches;
         check(cudaGetLastError(), "energy launch");
@@ -485,6 +515,8 @@ dp_status dp_sim_is_finite(dp_sim *sim, int32_t *finite) {
 int32_t dp_sim_is_reversible(const dp_sim *sim) { return sim && sim->scene.reversible ? 1 : 0; }
 
 uint32_t dp_sim_kernel(const dp_sim *sim) { return sim ? sim->kernel : 0; }
+
+uint32_t dp_sim_row_pitch(const dp_sim *sim) { return sim ? sim->pitch : 0; }
 
 uint64_t dp_sim_launch_count(const dp_sim *sim) { return sim ? sim->launches : 0; }
 

@@ -276,7 +276,9 @@ dp_status dp_sim_set_accumulate_intensity(dp_sim *sim, int on);
 uint64_t dp_sim_accumulated_steps(const dp_sim *sim);
 /* electric_buffer / magnetic_buffer / intensity_buffer (src/gpu.rs:366-374,
  * 596-599): the live device allocation, valid until the next advance,
- * reverse or destroy. */
+ * reverse or destroy.  Rows are dp_sim_row_pitch cells apart (nx rounded up
+ * to a multiple of 4, so equal to nx — the reference's dense layout — when nx
+ * is a multiple of 4); component a starts at a * pitch * ny * nz. */
 dp_status dp_sim_device_ptr(dp_sim *sim, uint32_t field, void **ptr);
 /* The simulation's CUDA stream (cudaStream_t), for zero-copy consumers. */
 dp_status dp_sim_stream(dp_sim *sim, void **stream);
@@ -348,6 +350,8 @@ uint64_t dp_batch_launch_count(const dp_batch *batch);
 dp_status dp_energy_noalloc(const float *electric, const float *magnetic, const uint8_t *material_index,
                             const float *eps_mu, const float *primary, const float *dual,
                             const uint32_t extent[3], double *out, void *stream);
+/* Row stride of the device field buffers, in cells. */
+uint32_t dp_sim_row_pitch(const dp_sim *sim);
 /* Kernel the handle actually runs (DP_KERNEL_FUSED or DP_KERNEL_NAIVE). */
 uint32_t dp_sim_kernel(const dp_sim *sim);
 /* Kernel launches issued by this handle so far (every kernel of this library). */

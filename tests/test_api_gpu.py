@@ -87,3 +87,22 @@ def test_device_pointer_and_bytes_per_step():
     sim.advance_by(5)
     sim.wait(10_000)
     assert sim.launch_count() > 0
+
+
+def test_grids_whose_rows_are_not_a_multiple_of_4_cells_run_fused_with_a_pitch():
+    """nx = 81: the device rows are padded to 84 cells; reads, writes and
+    restores go through the dense host layout unchanged."""
+    from tests import scenes
+    import oracle
+    scene, steps = scenes.graded()
+    sim = Simulation(scene)
+    assert sim.kernel == 1 and sim.extent[0] == 81
+    assert _abi.lib().dp_sim_row_pitch(sim.handle) == 84
+    sim.advance_by(40)
+    snap = sim.snapshot()
+    sim.advance_by(10)
+    sim.restore(snap)
+    sim.advance_by(10)
+    ref = oracle.OracleSimulation(scene, threads=8)
+    ref.advance_by(50)
+    assert np.array_equal(sim.read_electric().view(np.uint32), ref.read_electric().view(np.uint32))

@@ -20,16 +20,7 @@ TOLERANCE = 1e-5
 KERNELS = {"naive": DP_KERNEL_NAIVE, "fused": DP_KERNEL_FUSED}
 
 
-def fused_covers(scene) -> bool:
-    return scene.grid.extent.x % 4 == 0
-
-
 def run_pair(scene, steps, kernel, threads):
-    if kernel == DP_KERNEL_FUSED and not fused_covers(scene):
-        # The fused kernel's TMA rows need a 16-byte stride; AUTO runs the
-        # naive passes on such grids, and those are tested under "naive".
-        assert Simulation(scene).kernel == DP_KERNEL_NAIVE
-        pytest.skip("fused step needs nx % 4 == 0; AUTO uses the naive passes here")
     reference = oracle.OracleSimulation(scene, threads=threads)
     candidate = Simulation(scene, kernel=kernel)
     assert candidate.kernel == kernel
