@@ -53,6 +53,10 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--variant", default="", help="fused kernel cx,tile_y,slots (default: tuned)")
     p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-batched", action="store_true", help="skip the mixed-size batch measurement")
+    p.add_argument("--workload", choices=["heterogeneous", "batched", "served"], default="heterogeneous")
+    p.add_argument("--scenes", type=int, default=256, help="batched: scenes per batch")
+    p.add_argument("--batch-steps", type=int, default=1000, help="batched: steps per scene")
     return p.parse_args()
 
 
@@ -282,13 +286,21 @@ def run_ours(args):
         rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=12.0, max_steps=200, warmup=0)
         cpu = {"value": rate, "unit": "Gcell/s", "cores": threads, "kind": "port",
                "sample": f"{steps} oracle steps of the same {args.side}^3 scene, {elapsed:.1f} s"}
+    kernel_name = ["", "fused", "naive"][sim.kernel]
+    batched = None
+    if world == 1 and not args.no_batched:
+        sim.close()
+        try:
+            batched = batched_measurement(args.scenes, args.batch_steps, device)
+        except Exception as exc:  # reported, not fatal to the headline line
+            batched = {"error": f"{type(exc).__name__}: {exc}"}
     line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64 scene)",
-            "config": config(args.side, world), "kernel": ["", "fused", "naive"][sim.kernel],
+            "config": config(args.side, world), "kernel": kernel_name,
             "variant": args.variant or "default",
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clocks.summary()}
+            "clocks": clocks.summary(), "batched": batched}
     print(json.dumps(line), flush=True)
 
 
@@ -308,10 +320,62 @@ def read_into(sim, intensity, electric, magnetic) -> None:
     _abi.check(lib.dp_sim_read_field(sim.handle, _abi.DP_FIELD_MAGNETIC, magnetic.data_ptr(), magnetic.numel()))
 
 
+BATCH_SEED = 0xBA7C_0000
+
+
+def batched_measurement(scene_count: int, steps: int, device: int = 0) -> dict:
+    """Mixed-size batch vs this project's plain one-scene-at-a-time solver.
+
+    Scenes: axes log-uniform in [32, 160] cells, seeded spheres, an optional
+    conductor, one point or plane-wave source each (workloads.mixed_scene).
+    Host scene setup is done up front for both; each arm's clock covers
+    allocation, upload, stepping and reading every scene's E field back."""
+    import numpy as np
+    from diaphane_gb300 import Batch, ResolvedScene, Simulation, workloads
+    resolved = [ResolvedScene(workloads.mixed_scene(BATCH_SEED + k)) for k in range(scene_count)]
+    cells = sum(r.cells for r in resolved)
+    # Plain: one Simulation per scene, one after another.
+    plain_out = {}
+    t0 = time.perf_counter()
+    for k, r in enumerate(resolved):
+        sim = Simulation(r, device=device)
+        sim.advance_by(steps)
+        e = sim.read_electric()
+        if k < 4:
+            plain_out[k] = e
+        sim.close()
+    plain_s = time.perf_counter() - t0
+    # Batched: one arena, one launch per step per kernel variant, K-step graphs.
+    arena = int(1.05 * sum(Batch.bytes_for(r, steps) for r in resolved)) + (64 << 20)
+    batch = Batch(arena, chunk_steps=50, max_scenes=scene_count, device=device)
+    t0 = time.perf_counter()
+    ids = [batch.add(r, steps) for r in resolved]
+    batch.run_to_completion()
+    outs = [batch.read_electric(i) for i in ids]
+    batched_s = time.perf_counter() - t0
+    identical = all(np.array_equal(outs[k].view(np.uint32), plain_out[k].view(np.uint32)) for k in plain_out)
+    return {"scenes": scene_count, "steps": steps, "cells": cells,
+            "batched_solves_per_s": scene_count / batched_s, "plain_solves_per_s": scene_count / plain_s,
+            "speedup": plain_s / batched_s, "batched_gcells": cells * steps / batched_s / 1e9,
+            "plain_gcells": cells * steps / plain_s / 1e9, "batched_s": batched_s, "plain_s": plain_s,
+            "chunk_steps": 50, "graph_launches": batch.launch_count(),
+            "bit_identical_to_plain": identical}
+
+
+def run_batched(args):
+    line = {"metric": "solves/s (batched mixed sizes)", "workload": "batched"}
+    line.update(batched_measurement(args.scenes, args.batch_steps))
+    line["value"] = line["batched_solves_per_s"]
+    line["unit"] = "solves/s"
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batched":
+        run_batched(args)
     else:
         run_ours(args)
 
