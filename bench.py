@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--workload", choices=["heterogeneous", "batched", "served"], default="heterogeneous")
     p.add_argument("--scenes", type=int, default=256, help="batched: scenes per batch")
     p.add_argument("--batch-steps", type=int, default=1000, help="batched: steps per scene")
+    p.add_argument("--rates", default="4,16,64", help="served: arrival rates to sweep, requests/s")
+    p.add_argument("--requests", type=int, default=48, help="served: requests per trace")
     return p.parse_args()
 
 
@@ -370,12 +372,51 @@ def run_batched(args):
     print(json.dumps(line), flush=True)
 
 
+def served_measurement(rates, count: int, device: int = 0, arena_bytes: int = 150 * 10**9) -> list:
+    """Poisson arrival traces replayed twice each: continuous batching over
+    one arena (admission by bytes, join and leave at 50-step chunk
+    boundaries, 8 probes of Ez/Hy per step) and the plain solver, first come
+    first served.  Scene axes log-uniform in [48, 320] cells, steps uniform in
+    [200, 5000].  Latency = completion (results on the host) - arrival."""
+    from diaphane_gb300.serve import Server, poisson_trace, serve_plain, summary
+    server = Server(arena_bytes, max_scenes=256, chunk_steps=50, device=device)
+    warm = dict(lo=48, hi=64, steps=(50, 60))
+    server.serve(poisson_trace(2, 100.0, seed=1, **warm))
+    serve_plain(poisson_trace(2, 100.0, seed=1, **warm), device)
+    out = []
+    for rate in rates:
+        trace = server.serve(poisson_trace(count, rate))
+        served = summary(trace)
+        served["chunks"] = server.chunks
+        served["peak_active"] = server.peak_active
+        plain = summary(serve_plain(poisson_trace(count, rate), device))
+        out.append({"arrivals_per_s": rate, "served": served, "plain": plain,
+                    "p99_ratio_plain_over_served": plain["p99_s"] / served["p99_s"],
+                    "throughput_ratio": served["solves_per_s"] / plain["solves_per_s"]})
+        server.chunks = 0
+        server.peak_active = 0
+    server.close()
+    return out
+
+
+def run_served(args):
+    rates = [float(r) for r in args.rates.split(",")]
+    results = served_measurement(rates, args.requests)
+    top = results[-1]["served"]
+    line = {"metric": "solves/s (served, Poisson arrivals)", "workload": "served", "value": top["solves_per_s"],
+            "unit": "solves/s", "requests_per_trace": args.requests, "arena_bytes": 150 * 10**9,
+            "scene_axes": [48, 320], "steps": [200, 5000], "probes": 8, "by_rate": results}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "served":
+        run_served(args)
     else:
         run_ours(args)
 

@@ -1,0 +1,58 @@
+"""The served form: requests arrive over time, join a running batch at chunk
+boundaries and leave when done.  Every request's probe series (Ez and Hy at
+each probe cell after each step) must equal the oracle's run of that request
+alone, whatever it shared the batch with."""
+import numpy as np
+import pytest
+
+import oracle
+from diaphane_gb300.serve import Server, poisson_trace, serve_plain, summary
+from diaphane_gb300.workloads import mixed_scene
+
+pytestmark = pytest.mark.gpu
+
+
+def oracle_series(request, threads):
+    ref = oracle.OracleSimulation(mixed_scene(request.seed, request.lo, request.hi), threads=threads)
+    out = np.empty((request.steps, len(request.probes), 2), dtype=np.float32)
+    for t in range(request.steps):
+        ref.advance()
+        for k, p in enumerate(request.probes):
+            out[t, k, 0] = ref.sample_electric(2, p)
+            out[t, k, 1] = ref.sample_magnetic(1, p)
+    return out
+
+
+def test_requests_served_in_a_mix_match_each_run_alone(threads):
+    trace = poisson_trace(6, rate=150.0, seed=0x7E57, lo=36, hi=60, steps=(40, 130), probe_count=4)
+    server = Server(2 << 30, max_scenes=8, chunk_steps=16)
+    server.serve(trace)
+    assert server.peak_active >= 2  # the requests overlapped
+    for r in trace:
+        assert r.done is not None and r.done >= r.arrival
+        assert r.series.shape == (r.steps, 4, 2)
+        ref = oracle_series(r, threads)
+        assert np.array_equal(r.series.view(np.uint32), ref.view(np.uint32)), r.ident
+    used, _ = server.batch.memory()
+    assert used == 0  # every request left and gave its bytes back
+    server.close()
+
+
+def test_admission_waits_for_bytes_to_free():
+    """An arena that holds one request at a time serves them one after another."""
+    trace = poisson_trace(3, rate=1000.0, seed=0xADD, lo=40, hi=48, steps=(30, 40), probe_count=2)
+    for r in trace:
+        r.resolve()
+    from diaphane_gb300 import Batch
+    biggest = max(Batch.bytes_for(r.resolved, r.steps, len(r.probes)) for r in trace)
+    server = Server(biggest + (1 << 20), max_scenes=4, chunk_steps=8)
+    server.serve(trace)
+    assert server.peak_active == 1
+    assert all(r.series is not None and r.series.shape[0] == r.steps for r in trace)
+    server.close()
+
+
+def test_plain_replay_and_summary():
+    trace = serve_plain(poisson_trace(3, rate=1000.0, seed=0x9A1, lo=32, hi=40, steps=(20, 30)))
+    s = summary(trace)
+    assert s["requests"] == 3 and s["solves_per_s"] > 0 and s["p99_s"] >= s["p50_s"] > 0
