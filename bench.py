@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--variant", default="", help="fused kernel cx,tile_y,slots (default: tuned)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the mixed-size batch measurement")
-    p.add_argument("--workload", choices=["heterogeneous", "batched", "served"], default="heterogeneous")
+    p.add_argument("--workload", choices=["heterogeneous", "batched", "served", "accuracy"], default="heterogeneous")
     p.add_argument("--scenes", type=int, default=256, help="batched: scenes per batch")
     p.add_argument("--batch-steps", type=int, default=1000, help="batched: steps per scene")
     p.add_argument("--rates", default="4,16,64", help="served: arrival rates to sweep, requests/s")
@@ -409,6 +409,84 @@ def run_served(args):
     print(json.dumps(line), flush=True)
 
 
+def field_error(a32, b64, chunk: int = 1 << 24) -> dict:
+    """f32 field against its FP64 counterpart: max |difference| as a
+    fraction of the FP64 peak, and the relative L2 norm."""
+    import numpy as np
+    peak = worst = sd = sb = 0.0
+    for i in range(0, b64.size, chunk):
+        y = b64[i:i + chunk]
+        d = a32[i:i + chunk].astype(np.float64) - y
+        worst = max(worst, float(np.abs(d).max()))
+        peak = max(peak, float(np.abs(y).max()))
+        sd += float(np.dot(d, d))
+        sb += float(np.dot(y, y))
+    return {"max_abs_over_peak": worst / peak if peak else None, "rel_l2": (sd / sb) ** 0.5 if sb else None,
+            "peak": peak}
+
+
+def accuracy_case(name: str, scene, steps: int, device: int = 0) -> dict:
+    """The product's f32 step against the FP64 instance on the GPU, same
+    scene, same step count."""
+    from diaphane_gb300 import ResolvedScene, Simulation, Simulation64
+    resolved = ResolvedScene(scene)
+    f32 = Simulation(resolved, device=device)
+    f64 = Simulation64(resolved, device=device)
+    t0 = time.perf_counter()
+    f32.advance_by(steps)
+    f32.wait(600_000)
+    t32 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    f64.advance_by(steps)
+    f64.wait(1_800_000)
+    t64 = time.perf_counter() - t0
+    e32, e64 = f32.energy().total(), f64.energy().total()
+    out = {"case": name, "extent": list(resolved.extent), "steps": steps,
+           "E": field_error(f32.read_electric(), f64.read_electric()),
+           "H": field_error(f32.read_magnetic(), f64.read_magnetic()),
+           "energy_rel_diff": abs(e32 - e64) / e64 if e64 else None,
+           "f32_kernel": ["", "fused", "naive"][f32.kernel], "f32_s": t32, "f64_s": t64}
+    f32.close()
+    f64.close()
+    return out
+
+
+def drift_case(device: int = 0, early: int = 400, late: int = 20_000, window: int = 200) -> dict:
+    """Windowed-mean energy drift of the 192³ graded conducting box: mean
+    total energy over `window` steps after `early` steps, again after `late`
+    more, for the f32 step and the FP64 instance."""
+    from diaphane_gb300 import ResolvedScene, Simulation, Simulation64, workloads
+    resolved = ResolvedScene(workloads.graded_cavity())
+
+    def mean_energy(sim):
+        total = 0.0
+        for _ in range(window):
+            sim.advance_by(1)
+            total += sim.energy().total()
+        return total / window
+
+    out = {"case": "graded cavity (PEC)", "extent": list(resolved.extent), "early": early, "late": late,
+           "window": window}
+    for name, sim in (("f32", Simulation(resolved, device=device)), ("f64", Simulation64(resolved, device=device))):
+        sim.advance_by(early)
+        a = mean_energy(sim)
+        sim.advance_by(late)
+        b = mean_energy(sim)
+        out[f"drift_{name}"] = abs(b - a) / a
+        sim.close()
+    return out
+
+
+def run_accuracy(args):
+    from diaphane_gb300 import workloads
+    cases = [accuracy_case("free flight 80^3", workloads.free_flight(80), 1000),
+             accuracy_case("heterogeneous 512^3", workloads.heterogeneous(512), 2000),
+             accuracy_case("graded stack 640x256x256", workloads.graded_stack(), 5000)]
+    line = {"metric": "f32 error against the FP64 instance", "workload": "accuracy", "cases": cases,
+            "drift": drift_case()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -417,6 +495,8 @@ def main():
         run_batched(args)
     elif args.workload == "served":
         run_served(args)
+    elif args.workload == "accuracy":
+        run_accuracy(args)
     else:
         run_ours(args)
 

@@ -7,12 +7,12 @@ scene-authoring model that mirrors the reference's Rust types.
 from ._abi import DiaphaneError, DP_KERNEL_AUTO, DP_KERNEL_FUSED, DP_KERNEL_NAIVE
 from .scene import (Axis, Boundary, Extent, Grid, Material, MaterialTable, Refinement, Scene, Shape, Source,
                     Waveform, COURANT_LIMIT, SPEED_OF_LIGHT)
-from .simulation import Energy, ResolvedScene, Simulation, Snapshot
+from .simulation import Energy, ResolvedScene, Simulation, Simulation64, Snapshot
 from .batch import Batch
 from .timeline import Seek, Timeline
 
 __all__ = [
     "Axis", "Batch", "Boundary", "COURANT_LIMIT", "DiaphaneError", "DP_KERNEL_AUTO", "DP_KERNEL_FUSED", "DP_KERNEL_NAIVE",
     "Energy", "Extent", "Grid", "Material", "MaterialTable", "Refinement", "ResolvedScene", "Scene", "Seek",
-    "Shape", "Simulation", "Snapshot", "SPEED_OF_LIGHT", "Source", "Timeline", "Waveform",
+    "Shape", "Simulation", "Simulation64", "Snapshot", "SPEED_OF_LIGHT", "Source", "Timeline", "Waveform",
 ]

@@ -144,6 +144,13 @@ SIGNATURES = [
     ("dp_sim_kernel", C.c_uint32, [_P]),
     ("dp_sim_row_pitch", C.c_uint32, [_P]),
     ("dp_sim_launch_count", C.c_uint64, [_P]),
+    ("dp_sim64_create", C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
+    ("dp_sim64_destroy", None, [_P]),
+    ("dp_sim64_advance", C.c_int, [_P, C.c_uint64]),
+    ("dp_sim64_wait", C.c_int, [_P, C.c_uint32]),
+    ("dp_sim64_step_count", C.c_uint64, [_P]),
+    ("dp_sim64_read_field", C.c_int, [_P, C.c_uint32, _P, C.c_size_t]),
+    ("dp_sim64_energy", C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 ]
 
 

@@ -42,20 +42,30 @@ struct InjectionTable {
     DeviceInjection item[kMaxInjections];
 };
 
-// Fields of one buffer set: component a of E at e + a*cells.
-struct FieldSet {
-    float *e;
-    float *h;
+// Fields of one buffer set: component a of E at e + a*cells.  The step runs
+// in float; the FP64 instance keeps its fields in double.
+template <typename T> struct Fields {
+    T *e;
+    T *h;
 };
+using FieldSet = Fields<float>;
+using FieldSet64 = Fields<double>;
 
-// Naive path (kernels_naive.cu): one thread per cell, separate passes.
+// Naive path (kernels_naive.cu): one thread per cell, separate passes, in
+// float or (the FP64 instance) double.
 void launch_naive_magnetic(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream);
+void launch_naive_magnetic(const DeviceScene &s, FieldSet64 f, bool reverse, cudaStream_t stream);
 void launch_naive_electric(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream);
+void launch_naive_electric(const DeviceScene &s, FieldSet64 f, bool reverse, cudaStream_t stream);
 void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj, float sign, cudaStream_t stream);
+// `value` is the signed drive in double; inj.value is not read.
+void launch_inject(const DeviceScene &s, FieldSet64 f, const DeviceInjection &inj, double value, cudaStream_t stream);
 void launch_intensity(const DeviceScene &s, const float *e, float *intensity, cudaStream_t stream);
 
 // Reductions (kernels_naive.cu).
 void launch_energy(const DeviceScene &s, FieldSet f, const float *primary, const float *dual,
+                   const float2 *eps_mu, double *partials, uint32_t blocks, cudaStream_t stream);
+void launch_energy(const DeviceScene &s, FieldSet64 f, const float *primary, const float *dual,
                    const float2 *eps_mu, double *partials, uint32_t blocks, cudaStream_t stream);
 void launch_finite(const DeviceScene &s, FieldSet f, int32_t *flag, cudaStream_t stream);
 uint32_t energy_blocks(uint64_t cells);

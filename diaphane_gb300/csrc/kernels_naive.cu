@@ -1,10 +1,11 @@
 // One-thread-per-cell kernels: the H pass, the E pass, an injection pass,
-// the intensity pass, and the energy / finiteness reductions.
+// the intensity pass, and the energy / finiteness reductions; the H, E,
+// injection and energy passes also in double for the FP64 instance.
 //
 // These mirror the reference step's structure (src/cpu.rs:174-198) pass for
-// pass and are kept for three jobs: the exact inverse step (reverse_by), the
-// small-grid fallback the fused kernel does not cover, and an independent
-// second implementation the fused kernel is checked against.
+// pass and are kept for four jobs: the exact inverse step (reverse_by), the
+// fallback for scenes the fused kernel does not cover, an independent second
+// implementation the fused kernel is checked against, and the FP64 instance.
 #include "device.cuh"
 
 namespace diaphane {
@@ -31,10 +32,12 @@ __device__ __forceinline__ float profile(const float *absorber, uint32_t span, c
 
 // update_magnetic (src/cpu.rs:283-376) and reverse_magnetic (:490-572) for
 // every cell at once: the bulk sweep and the two high-wall planes are the same
-// expression with the missing forward neighbour read as the wall's zero.
-template <bool Reverse>
-__global__ void __launch_bounds__(kThreads) magnetic_pass(DeviceScene s, const float *__restrict__ e,
-                                                          float *__restrict__ h) {
+// expression with the missing forward neighbour read as the wall's zero.  In
+// double (T) the gains, losses and coefficients are the f32 setup values
+// promoted, and the loss is summed in f32 as the setup tables are.
+template <typename T, bool Reverse>
+__global__ void __launch_bounds__(kThreads) magnetic_pass(DeviceScene s, const T *__restrict__ e,
+                                                          T *__restrict__ h) {
     const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
     if (i >= s.cells) return;
     uint32_t c[3];
@@ -46,30 +49,30 @@ __global__ void __launch_bounds__(kThreads) magnetic_pass(DeviceScene s, const f
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const int b = (a + 1) % 3, cc = (a + 2) % 3;
-        const float *ec = e + uint64_t(cc) * s.cells;
-        const float *eb = e + uint64_t(b) * s.cells;
-        const float next_c = c[b] + 1 < s.n[b] ? ec[i + stride[b]] : 0.0f;
-        const float next_b = c[cc] + 1 < s.n[cc] ? eb[i + stride[cc]] : 0.0f;
-        const float curl = __ldg(&s.mgain[offset[b] + c[b]]) * (next_c - ec[i]) -
-                           __ldg(&s.mgain[offset[cc] + c[cc]]) * (next_b - eb[i]);
+        const T *ec = e + uint64_t(cc) * s.cells;
+        const T *eb = e + uint64_t(b) * s.cells;
+        const T next_c = c[b] + 1 < s.n[b] ? ec[i + stride[b]] : T(0);
+        const T next_b = c[cc] + 1 < s.n[cc] ? eb[i + stride[cc]] : T(0);
+        const T curl = T(__ldg(&s.mgain[offset[b] + c[b]])) * (next_c - ec[i]) -
+                       T(__ldg(&s.mgain[offset[cc] + c[cc]])) * (next_b - eb[i]);
         // magnetic_row: the integer profile along a, half along the others.
         const float row = profile(s.absorber, span, offset, 1, c[1], a != 1) +
                           profile(s.absorber, span, offset, 2, c[2], a != 2);
-        const float loss = (k.w + row) + profile(s.absorber, span, offset, 0, c[0], a != 0);
-        float *target = h + uint64_t(a) * s.cells + i;
-        const float old = *target;
+        const T loss = T((k.w + row) + profile(s.absorber, span, offset, 0, c[0], a != 0));
+        T *target = h + uint64_t(a) * s.cells + i;
+        const T old = *target;
         if (Reverse)
-            *target = ((1.0f + loss) * old + k.z * curl) / (1.0f - loss);
+            *target = ((T(1) + loss) * old + T(k.z) * curl) / (T(1) - loss);
         else
-            *target = ((1.0f - loss) * old - k.z * curl) / (1.0f + loss);
+            *target = ((T(1) - loss) * old - T(k.z) * curl) / (T(1) + loss);
     }
 }
 
 // update_electric (src/cpu.rs:380-434) and reverse_electric (:441-487).
 // Index 0 along b or c is never written: the low-wall conductor.
-template <bool Reverse>
-__global__ void __launch_bounds__(kThreads) electric_pass(DeviceScene s, const float *__restrict__ h,
-                                                          float *__restrict__ e) {
+template <typename T, bool Reverse>
+__global__ void __launch_bounds__(kThreads) electric_pass(DeviceScene s, const T *__restrict__ h,
+                                                          T *__restrict__ e) {
     const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
     if (i >= s.cells) return;
     uint32_t c[3];
@@ -82,25 +85,27 @@ __global__ void __launch_bounds__(kThreads) electric_pass(DeviceScene s, const f
     for (int a = 0; a < 3; ++a) {
         const int b = (a + 1) % 3, cc = (a + 2) % 3;
         if (c[b] == 0 || c[cc] == 0) continue;
-        const float *hc = h + uint64_t(cc) * s.cells;
-        const float *hb = h + uint64_t(b) * s.cells;
-        const float curl = __ldg(&s.egain[offset[b] + c[b]]) * (hc[i] - hc[i - stride[b]]) -
-                           __ldg(&s.egain[offset[cc] + c[cc]]) * (hb[i] - hb[i - stride[cc]]);
+        const T *hc = h + uint64_t(cc) * s.cells;
+        const T *hb = h + uint64_t(b) * s.cells;
+        const T curl = T(__ldg(&s.egain[offset[b] + c[b]])) * (hc[i] - hc[i - stride[b]]) -
+                       T(__ldg(&s.egain[offset[cc] + c[cc]])) * (hb[i] - hb[i - stride[cc]]);
         // electric_row: the half profile along a, integer along the others.
         const float row = profile(s.absorber, span, offset, 1, c[1], a == 1) +
                           profile(s.absorber, span, offset, 2, c[2], a == 2);
-        const float loss = (k.y + row) + profile(s.absorber, span, offset, 0, c[0], a == 0);
-        float *target = e + uint64_t(a) * s.cells + i;
-        const float old = *target;
+        const T loss = T((k.y + row) + profile(s.absorber, span, offset, 0, c[0], a == 0));
+        T *target = e + uint64_t(a) * s.cells + i;
+        const T old = *target;
         if (Reverse)
-            *target = ((1.0f + loss) * old - k.x * curl) / (1.0f - loss);
+            *target = ((T(1) + loss) * old - T(k.x) * curl) / (T(1) - loss);
         else
-            *target = ((1.0f - loss) * old + k.x * curl) / (1.0f + loss);
+            *target = ((T(1) - loss) * old + T(k.x) * curl) / (T(1) + loss);
     }
 }
 
-// One soft injection over its box (fdtd.wgsl inject, src/cpu.rs:618-629).
-__global__ void __launch_bounds__(kThreads) inject_pass(DeviceScene s, FieldSet f, DeviceInjection inj, float sign) {
+// One soft injection over its box (fdtd.wgsl inject, src/cpu.rs:618-629);
+// `value` is the drive with its sign applied.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) inject_pass(DeviceScene s, Fields<T> f, DeviceInjection inj, T value) {
     const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
     const uint64_t count = uint64_t(inj.extent[0]) * inj.extent[1] * inj.extent[2];
     if (i >= count) return;
@@ -110,8 +115,8 @@ __global__ void __launch_bounds__(kThreads) inject_pass(DeviceScene s, FieldSet 
     const uint32_t dz = uint32_t(t / inj.extent[1]);
     const uint64_t cell = (uint64_t(inj.origin[2] + dz) * s.n[1] + (inj.origin[1] + dy)) * s.pitch + inj.origin[0] + dx;
     const float weight = inj.weight_offset < 0 ? 1.0f : __ldg(&s.weights[inj.weight_offset + i]);
-    float *field = (inj.magnetic ? f.h : f.e) + uint64_t(inj.component) * s.cells;
-    field[cell] += (sign * inj.value) * weight;
+    T *field = (inj.magnetic ? f.h : f.e) + uint64_t(inj.component) * s.cells;
+    field[cell] += value * T(weight);
 }
 
 // I += Ex² + Ey² + Ez² (src/cpu.rs:186-196).
@@ -128,7 +133,8 @@ __global__ void __launch_bounds__(kThreads) intensity_pass(DeviceScene s, const 
 
 // energy (src/cpu.rs:654-687): each component integrated over its own box,
 // accumulated in f64.  One partial pair per block; the host adds them.
-__global__ void __launch_bounds__(kThreads) energy_pass(DeviceScene s, FieldSet f, const float *__restrict__ primary,
+template <typename T>
+__global__ void __launch_bounds__(kThreads) energy_pass(DeviceScene s, Fields<T> f, const float *__restrict__ primary,
                                                         const float *__restrict__ dual,
                                                         const float2 *__restrict__ eps_mu, double *partials) {
     const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
@@ -141,14 +147,14 @@ __global__ void __launch_bounds__(kThreads) energy_pass(DeviceScene s, FieldSet 
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const int b = (a + 1) % 3, cc = (a + 2) % 3;
-            const float ev = f.e[uint64_t(a) * s.cells + i];
-            const float hv = f.h[uint64_t(a) * s.cells + i];
+            const T ev = f.e[uint64_t(a) * s.cells + i];
+            const T hv = f.h[uint64_t(a) * s.cells + i];
             const double volume_e = double(primary[offset[a] + c[a]]) * double(dual[offset[b] + c[b]]) *
                                     double(dual[offset[cc] + c[cc]]);
             const double volume_h = double(dual[offset[a] + c[a]]) * double(primary[offset[b] + c[b]]) *
                                     double(primary[offset[cc] + c[cc]]);
-            ee += 0.5 * volume_e * double(m.x * ev * ev);
-            em += 0.5 * volume_h * double(m.y * hv * hv);
+            ee += 0.5 * volume_e * double(T(m.x) * ev * ev);
+            em += 0.5 * volume_h * double(T(m.y) * hv * hv);
         }
     }
     __shared__ double se[kThreads], sm[kThreads];
@@ -181,24 +187,50 @@ uint32_t blocks_for(uint64_t n) { return uint32_t((n + kThreads - 1) / kThreads)
 
 } // namespace
 
-void launch_naive_magnetic(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream) {
+namespace {
+
+template <typename T> void magnetic(const DeviceScene &s, Fields<T> f, bool reverse, cudaStream_t stream) {
     if (reverse)
-        magnetic_pass<true><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.e, f.h);
+        magnetic_pass<T, true><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.e, f.h);
     else
-        magnetic_pass<false><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.e, f.h);
+        magnetic_pass<T, false><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.e, f.h);
 }
 
-void launch_naive_electric(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream) {
+template <typename T> void electric(const DeviceScene &s, Fields<T> f, bool reverse, cudaStream_t stream) {
     if (reverse)
-        electric_pass<true><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.h, f.e);
+        electric_pass<T, true><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.h, f.e);
     else
-        electric_pass<false><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.h, f.e);
+        electric_pass<T, false><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.h, f.e);
 }
 
-void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj, float sign, cudaStream_t stream) {
+template <typename T> void inject(const DeviceScene &s, Fields<T> f, const DeviceInjection &inj, T value,
+                                  cudaStream_t stream) {
     const uint64_t count = uint64_t(inj.extent[0]) * inj.extent[1] * inj.extent[2];
     if (count == 0) return;
-    inject_pass<<<blocks_for(count), kThreads, 0, stream>>>(s, f, inj, sign);
+    inject_pass<T><<<blocks_for(count), kThreads, 0, stream>>>(s, f, inj, value);
+}
+
+} // namespace
+
+void launch_naive_magnetic(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream) {
+    magnetic(s, f, reverse, stream);
+}
+void launch_naive_magnetic(const DeviceScene &s, FieldSet64 f, bool reverse, cudaStream_t stream) {
+    magnetic(s, f, reverse, stream);
+}
+void launch_naive_electric(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream) {
+    electric(s, f, reverse, stream);
+}
+void launch_naive_electric(const DeviceScene &s, FieldSet64 f, bool reverse, cudaStream_t stream) {
+    electric(s, f, reverse, stream);
+}
+
+// sign · value is exact (sign is ±1), so the f32 drive is the reference's.
+void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj, float sign, cudaStream_t stream) {
+    inject(s, f, inj, sign * inj.value, stream);
+}
+void launch_inject(const DeviceScene &s, FieldSet64 f, const DeviceInjection &inj, double value, cudaStream_t stream) {
+    inject(s, f, inj, value, stream);
 }
 
 void launch_intensity(const DeviceScene &s, const float *e, float *intensity, cudaStream_t stream) {
@@ -212,7 +244,11 @@ uint32_t energy_blocks(uint64_t cells) {
 
 void launch_energy(const DeviceScene &s, FieldSet f, const float *primary, const float *dual, const float2 *eps_mu,
                    double *partials, uint32_t blocks, cudaStream_t stream) {
-    energy_pass<<<blocks, kThreads, 0, stream>>>(s, f, primary, dual, eps_mu, partials);
+    energy_pass<float><<<blocks, kThreads, 0, stream>>>(s, f, primary, dual, eps_mu, partials);
+}
+void launch_energy(const DeviceScene &s, FieldSet64 f, const float *primary, const float *dual, const float2 *eps_mu,
+                   double *partials, uint32_t blocks, cudaStream_t stream) {
+    energy_pass<double><<<blocks, kThreads, 0, stream>>>(s, f, primary, dual, eps_mu, partials);
 }
 
 void launch_finite(const DeviceScene &s, FieldSet f, int32_t *flag, cudaStream_t stream) {

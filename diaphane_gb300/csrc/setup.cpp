@@ -224,30 +224,37 @@ bool ResolvedGrid::contains(const float position[3]) const {
     return true;
 }
 
+template <typename T> constexpr T pi_in();
+template <> constexpr float pi_in<float>() { return kPi; }
+template <> constexpr double pi_in<double>() { return 3.14159265358979323846; }
+
 // Waveform::evaluate, src/source.rs:74-115.
-float waveform_value(const dp_waveform &w, float t) {
+template <typename T> T waveform_in(const dp_waveform &w, T t) {
+    const T pi = pi_in<T>();
     switch (w.kind) {
     case DP_WAVE_RICKER: {
-        float arg = kPi * w.frequency * (t - w.delay);
-        float arg2 = arg * arg;
-        return (1.0f - 2.0f * arg2) * std::exp(-arg2);
+        T arg = pi * T(w.frequency) * (t - T(w.delay));
+        T arg2 = arg * arg;
+        return (T(1) - T(2) * arg2) * std::exp(-arg2);
     }
     case DP_WAVE_GAUSSIAN_PULSE: {
-        const float fwhm_to_sigma = 0.4246609f; // 1 / (2 sqrt(2 ln 2))
-        float sigma = fwhm_to_sigma * w.duration_cycles / w.frequency;
-        float tau = t - w.delay;
-        float envelope = std::exp(-0.5f * (tau / sigma) * (tau / sigma));
-        return envelope * std::sin(2.0f * kPi * w.frequency * tau);
+        const T fwhm_to_sigma = T(0.4246609f); // 1 / (2 sqrt(2 ln 2))
+        T sigma = fwhm_to_sigma * T(w.duration_cycles) / T(w.frequency);
+        T tau = t - T(w.delay);
+        T envelope = std::exp(T(-0.5) * (tau / sigma) * (tau / sigma));
+        return envelope * std::sin(T(2) * pi * T(w.frequency) * tau);
     }
     case DP_WAVE_CONTINUOUS: {
-        if (t <= 0.0f) return 0.0f;
-        float ramp = w.ramp_cycles / w.frequency;
-        float envelope = t >= ramp ? 1.0f : 0.5f * (1.0f - std::cos(kPi * t / ramp));
-        return envelope * std::sin(2.0f * kPi * w.frequency * t);
+        if (t <= T(0)) return T(0);
+        T ramp = T(w.ramp_cycles) / T(w.frequency);
+        T envelope = t >= ramp ? T(1) : T(0.5) * (T(1) - std::cos(pi * t / ramp));
+        return envelope * std::sin(T(2) * pi * T(w.frequency) * t);
     }
     }
-    return 0.0f;
+    return T(0);
 }
+template float waveform_in<float>(const dp_waveform &, float);
+template double waveform_in<double>(const dp_waveform &, double);
 
 // Injection::weight, src/source.rs:441-455.
 float injection_weight(const StepInjection &inj, const float position[3]) {
@@ -440,24 +447,24 @@ Scene Scene::build(const dp_scene_desc &d) {
 }
 
 // Source::injections, src/source.rs:280-403: two slots per source.
-void Scene::injections(float time, std::vector<StepInjection> &out) const {
+template <typename T> void Scene::injections_in(T time, std::vector<InjectionOf<T>> &out) const {
     out.clear();
     const ResolvedGrid &g = grid;
     for (size_t k = 0; k < sources.size(); ++k) {
         const dp_source &src = sources[k];
-        const float value = src.amplitude * waveform_value(src.waveform, time);
-        StepInjection a{}, b{};
+        const T value = T(src.amplitude) * waveform_in<T>(src.waveform, time);
+        InjectionOf<T> a{}, b{};
         a.weight_offset = b.weight_offset = -1;
         a.component = b.component = src.polarization;
         if (src.shape == DP_SOURCE_POINT) {
             float position[3];
-            for (int i = 0; i < 3; ++i) position[i] = src.at[i] + src.velocity[i] * time;
+            for (int i = 0; i < 3; ++i) position[i] = src.at[i] + src.velocity[i] * static_cast<float>(time);
             g.cell_containing(position, a.origin);
             a.extent[0] = a.extent[1] = a.extent[2] = 1;
             // A mover outside the domain is silent, not clamped.
-            a.value = g.contains(position) ? value : 0.0f;
+            a.value = g.contains(position) ? value : T(0);
             b = a;
-            b.value = 0.0f;
+            b.value = T(0);
         } else if (src.shape == DP_SOURCE_SHEET) {
             const int axis = int(src.axis);
             float position[3] = {0.0f, 0.0f, 0.0f};
@@ -474,7 +481,7 @@ void Scene::injections(float time, std::vector<StepInjection> &out) const {
             a.weight_offset = source_weight.empty() ? -1 : source_weight[k];
             a.value = value;
             b = a;
-            b.value = 0.0f;
+            b.value = T(0);
         } else {
             // Total-field / scattered-field plane, src/source.rs:334-401.
             const int travel = int(src.axis);
@@ -484,14 +491,14 @@ void Scene::injections(float time, std::vector<StepInjection> &out) const {
             g.cell_containing(position, cell);
             const uint32_t plane = std::max<uint32_t>(cell[travel], 1);
             const float spacing = g.axes[travel].finest();
-            const float dt_local = g.time_step();
-            const float gain = kSpeedOfLight * dt_local / spacing;
-            const float omega = 2.0f * kPi * src.waveform.frequency;
-            const float half_k_spacing = std::asin(std::sin(0.5f * omega * dt_local) / gain);
-            const float retard = half_k_spacing / omega;
+            const T dt_local = T(g.time_step());
+            const T gain = T(kSpeedOfLight * g.time_step() / spacing);
+            const T omega = T(2) * pi_in<T>() * T(src.waveform.frequency);
+            const T half_k_spacing = std::asin(std::sin(T(0.5) * omega * dt_local) / gain);
+            const T retard = half_k_spacing / omega;
             const int pol = int(src.polarization);
             const uint32_t h_axis = uint32_t(3 - travel - pol);
-            const float h_sign = ((pol + 1) % 3) == travel ? -1.0f : 1.0f;
+            const T h_sign = ((pol + 1) % 3) == travel ? T(-1) : T(1);
             for (int i = 0; i < 3; ++i) {
                 a.extent[i] = b.extent[i] = g.n[i];
             }
@@ -499,14 +506,17 @@ void Scene::injections(float time, std::vector<StepInjection> &out) const {
             a.extent[travel] = 1;
             b.origin[travel] = plane - 1;
             b.extent[travel] = 1;
-            a.value = gain * (src.amplitude * waveform_value(src.waveform, time - 0.5f * dt_local + retard));
+            a.value = gain * (T(src.amplitude) * waveform_in<T>(src.waveform, time - T(0.5) * dt_local + retard));
             b.component = h_axis;
             b.magnetic = 1;
-            b.value = h_sign * gain * (src.amplitude * waveform_value(src.waveform, time - dt_local));
+            b.value = h_sign * gain * (T(src.amplitude) * waveform_in<T>(src.waveform, time - dt_local));
         }
         out.push_back(a);
         out.push_back(b);
     }
 }
+
+template void Scene::injections_in<float>(float, std::vector<InjectionOf<float>> &) const;
+template void Scene::injections_in<double>(double, std::vector<InjectionOf<double>> &) const;
 
 } // namespace diaphane

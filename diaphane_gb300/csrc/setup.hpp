@@ -66,17 +66,20 @@ struct Coeff {
     float electric_gain, electric_loss, magnetic_gain, magnetic_loss;
 };
 
-// One injection slot for one step, ready for a kernel.
-struct StepInjection {
+// One injection slot for one step, ready for a kernel.  T is the type the
+// drive value is computed in: f32 for the step itself, f64 for the FP64
+// instance (positions and weights stay f32 setup values in both).
+template <typename T> struct InjectionOf {
     uint32_t origin[3];
     uint32_t extent[3];
     uint32_t component;
     uint32_t magnetic;
-    float value;
+    T value;
     int32_t weight_offset; // into Scene::weights, -1 when every cell weighs 1
     float inverse_waist_squared;
     float center[3];
 };
+using StepInjection = InjectionOf<float>;
 
 // The resolved scene: the tables the kernels read.
 struct Scene {
@@ -108,10 +111,14 @@ struct Scene {
     uint32_t axis_offset(int axis) const { return axis == 0 ? 0 : (axis == 1 ? grid.n[0] : grid.n[0] + grid.n[1]); }
 
     // Source::injections for every source at `time`, two slots per source.
-    void injections(float time, std::vector<StepInjection> &out) const;
+    void injections(float time, std::vector<StepInjection> &out) const { injections_in<float>(time, out); }
+    // The same with time and drive in T (float and double are instantiated).
+    template <typename T> void injections_in(T time, std::vector<InjectionOf<T>> &out) const;
 };
 
-float waveform_value(const dp_waveform &w, float time);
+// Waveform::evaluate in T (float and double are instantiated).
+template <typename T> T waveform_in(const dp_waveform &w, T time);
+inline float waveform_value(const dp_waveform &w, float time) { return waveform_in<float>(w, time); }
 float injection_weight(const StepInjection &inj, const float position[3]);
 
 } // namespace diaphane

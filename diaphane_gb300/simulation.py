@@ -208,3 +208,49 @@ class Simulation:
         e = np.ascontiguousarray(snapshot.electric, dtype=np.float32)
         h = np.ascontiguousarray(snapshot.magnetic, dtype=np.float32)
         _abi.check(_abi.lib().dp_sim_restore(self.handle, snapshot.step, e.ctypes.data, h.ctypes.data, e.size))
+
+
+class Simulation64:
+    """The FP64 instance (dp_sim64): the same step in double on the GPU, the
+    run the f32 step's error is measured against."""
+
+    def __init__(self, scene: Scene | ResolvedScene, device: int = 0):
+        self.resolved = scene if isinstance(scene, ResolvedScene) else ResolvedScene(scene)
+        handle = C.c_void_p()
+        _abi.check(_abi.lib().dp_sim64_create(self.resolved.handle, device, C.byref(handle)))
+        self.handle = handle
+        self.extent = self.resolved.extent
+        self.cells = self.resolved.cells
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            _abi.lib().dp_sim64_destroy(self.handle)
+            self.handle = None
+
+    def close(self) -> None:
+        self.__del__()
+
+    def advance_by(self, steps: int) -> None:
+        _abi.check(_abi.lib().dp_sim64_advance(self.handle, steps))
+
+    def wait(self, timeout_ms: int = 600_000) -> None:
+        _abi.check(_abi.lib().dp_sim64_wait(self.handle, timeout_ms))
+
+    def step_count(self) -> int:
+        return _abi.lib().dp_sim64_step_count(self.handle)
+
+    def _read(self, field: int) -> np.ndarray:
+        out = np.empty(3 * self.cells, dtype=np.float64)
+        _abi.check(_abi.lib().dp_sim64_read_field(self.handle, field, out.ctypes.data, out.size))
+        return out
+
+    def read_electric(self) -> np.ndarray:
+        return self._read(_abi.DP_FIELD_ELECTRIC)
+
+    def read_magnetic(self) -> np.ndarray:
+        return self._read(_abi.DP_FIELD_MAGNETIC)
+
+    def energy(self) -> Energy:
+        e, m = C.c_double(), C.c_double()
+        _abi.check(_abi.lib().dp_sim64_energy(self.handle, C.byref(e), C.byref(m)))
+        return Energy(e.value, m.value)

@@ -161,3 +161,12 @@ def mixed_scene(seed: int, lo: int = 32, hi: int = 160, steps: int = 1000) -> Sc
         scene.sources.append(Source.plane_wave(Axis.X, float(f32(13.5) * cell - half[0]), Axis.Z,
                                                Waveform.gaussian_pulse(frequency, 3.0)))
     return scene
+
+
+def graded_cavity() -> Scene:
+    """192³ graded conducting box: 175.5 × 192 × 192 mm at 1 mm, x graded at
+    cap 1.15 down to 0.4 mm across an 8 mm band at the centre (192 cells
+    along x), perfectly conducting walls, a Ricker point source at 16 cells
+    per wavelength a sixth of the box from the centre (Scene::cavity_on)."""
+    grid = Grid.graded((0.1755, 0.192, 0.192), 1000.0, [Refinement.across(Axis.X, 0.0, 0.008, 4e-4)], 1.15)
+    return Scene.cavity_on(grid)

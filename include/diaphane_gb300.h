@@ -357,6 +357,24 @@ uint32_t dp_sim_kernel(const dp_sim *sim);
 /* Kernel launches issued by this handle so far (every kernel of this library). */
 uint64_t dp_sim_launch_count(const dp_sim *sim);
 
+/* ---- FP64 instance ------------------------------------------------------
+ * The same time step in double on the GPU: fields, curls, updates, drive
+ * values and time in f64 over the f32 setup tables, i.e. the reference's
+ * Simulation instantiated at f64 (src/cpu.rs:174-198, 283-434, 606-633 with
+ * T = f64).  It is what the f32 step's error is measured against; it has no
+ * reverse, intensity or fused path.  advance is asynchronous like
+ * dp_sim_advance; reads and the energy wait. */
+typedef struct dp_sim64 dp_sim64;
+dp_status dp_sim64_create(const dp_scene *scene, int32_t device, dp_sim64 **out);
+void dp_sim64_destroy(dp_sim64 *sim);
+dp_status dp_sim64_advance(dp_sim64 *sim, uint64_t steps);
+dp_status dp_sim64_wait(dp_sim64 *sim, uint32_t timeout_ms);
+uint64_t dp_sim64_step_count(const dp_sim64 *sim);
+/* DP_FIELD_ELECTRIC or DP_FIELD_MAGNETIC, 3 * cells doubles, component-major. */
+dp_status dp_sim64_read_field(dp_sim64 *sim, uint32_t field, double *host, size_t count);
+/* energy, src/cpu.rs:654-687, over the f64 fields. */
+dp_status dp_sim64_energy(dp_sim64 *sim, double *electric, double *magnetic);
+
 #ifdef __cplusplus
 }
 #endif
