@@ -144,6 +144,7 @@ SIGNATURES = [
     ("dp_sim_kernel", C.c_uint32, [_P]),
     ("dp_sim_row_pitch", C.c_uint32, [_P]),
     ("dp_sim_launch_count", C.c_uint64, [_P]),
+    ("dp_scene_raster", C.c_int, [_P, _P, C.c_uint32, _P]),
     ("dp_sim64_create", C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
     ("dp_sim64_destroy", None, [_P]),
     ("dp_sim64_advance", C.c_int, [_P, C.c_uint64]),

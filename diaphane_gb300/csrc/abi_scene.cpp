@@ -128,7 +128,7 @@ dp_status dp_scene_table(const dp_scene *scene, uint32_t table, void *host, size
         case DP_TABLE_CELL_CENTERS: src = s.centers.data(); size = s.centers.size() * 4; break;
         case DP_TABLE_ABSORBER: src = s.absorber.data(); size = s.absorber.size() * 4; break;
         case DP_TABLE_COEFFICIENTS: src = s.coefficients.data(); size = s.coefficients.size() * sizeof(Coeff); break;
-        case DP_TABLE_MATERIAL_INDEX: src = s.material_index.data(); size = s.material_index.size(); break;
+        case DP_TABLE_MATERIAL_INDEX: src = s.material_index().data(); size = s.material_index().size(); break;
         case DP_TABLE_PRIMARY: src = s.primary.data(); size = s.primary.size() * 4; break;
         case DP_TABLE_DUAL: src = s.dual.data(); size = s.dual.size() * 4; break;
         default: throw Error(DP_ERR_INVALID, "unknown table");

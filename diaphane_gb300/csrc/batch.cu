@@ -510,10 +510,7 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         // Zeroed fields; tables uploaded; the index padded row by row.
         cudaStream_t st = b->stream;
         check(cudaMemsetAsync(b->arena_base + offset, 0, 4 * l.fields + l.intensity, st), "zero fields");
-        const uint32_t nx = s.grid.n[0], rows = s.grid.n[1] * s.grid.n[2];
-        std::vector<uint8_t> padded(size_t(l.material_pitch) * rows, 0);
-        for (size_t r = 0; r < rows; ++r) std::memcpy(&padded[r * l.material_pitch], &s.material_index[r * nx], nx);
-        check(cudaMemcpyAsync(material, padded.data(), padded.size(), cudaMemcpyHostToDevice, st), "index");
+        rasterize_on_device(s, material, l.material_pitch, st);
         std::vector<float4> table(256, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         for (size_t m = 0; m < s.coefficients.size(); ++m)
             table[m] = make_float4(s.coefficients[m].electric_gain, s.coefficients[m].electric_loss,

@@ -62,6 +62,11 @@ void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj,
 void launch_inject(const DeviceScene &s, FieldSet64 f, const DeviceInjection &inj, double value, cudaStream_t stream);
 void launch_intensity(const DeviceScene &s, const float *e, float *intensity, cudaStream_t stream);
 
+// Scene::material_indices on the device (raster.cu): the u8 index with rows of
+// `pitch` bytes (padding cells 0), asynchronous on `stream`.
+struct Scene;
+void rasterize_on_device(const Scene &s, uint8_t *out, uint32_t pitch, cudaStream_t stream);
+
 // Reductions (kernels_naive.cu).
 void launch_energy(const DeviceScene &s, FieldSet f, const float *primary, const float *dual,
                    const float2 *eps_mu, double *partials, uint32_t blocks, cudaStream_t stream);

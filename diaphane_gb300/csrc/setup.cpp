@@ -280,6 +280,8 @@ Coeff material_coefficients(const dp_material &m, float dt) {
                  half_step * m.magnetic_loss / (kVacuumPermeability * m.relative_permeability)};
 }
 
+} // namespace
+
 // Shape::contains, src/scene.rs:60-81.
 bool shape_contains(const dp_shape &s, const float p[3]) {
     if (s.kind == DP_SHAPE_BLOCK) {
@@ -297,11 +299,13 @@ bool shape_contains(const dp_shape &s, const float p[3]) {
     return std::fabs(p[s.axis] - s.offset) <= 0.5f * s.thickness;
 }
 
+namespace {
+
 // Cells a shape can possibly cover along one axis: the cells containing its
 // two extremes, widened by two cells against rounding.  The exact membership
 // test runs on every cell in the range, so this only skips cells whose
 // centres lie well outside the shape (Shape::bounds, src/scene.rs:85-102).
-void shape_range(const ResolvedGrid &g, const dp_shape &s, int a, uint32_t &lo, uint32_t &hi) {
+void shape_range_impl(const ResolvedGrid &g, const dp_shape &s, int a, uint32_t &lo, uint32_t &hi) {
     float center = 0.0f, half = std::numeric_limits<float>::infinity();
     if (s.kind == DP_SHAPE_BLOCK) {
         center = s.center[a];
@@ -328,6 +332,44 @@ void shape_range(const ResolvedGrid &g, const dp_shape &s, int a, uint32_t &lo, 
 }
 
 } // namespace
+
+void shape_cell_range(const ResolvedGrid &g, const dp_shape &s, int axis, uint32_t &lo, uint32_t &hi) {
+    shape_range_impl(g, s, axis, lo, hi);
+}
+
+// Scene::material_indices, src/scene.rs:181-206: later shapes overwrite
+// earlier ones, membership decided at the cell centre.
+const std::vector<uint8_t> &Scene::material_index() const {
+    if (indexed_) return index_cache_;
+    const ResolvedGrid &g = grid;
+    index_cache_.assign(g.cells(), 0);
+    for (const dp_shape &sh : shapes) {
+        uint32_t lo[3], hi[3];
+        bool empty = false;
+        for (int a = 0; a < 3; ++a) {
+            shape_range_impl(g, sh, a, lo[a], hi[a]);
+            if (lo[a] > hi[a]) empty = true;
+        }
+        if (empty) continue;
+        const uint8_t material = uint8_t(sh.material);
+        const long z0 = lo[2], z1 = hi[2];
+#pragma omp parallel for schedule(dynamic, 1)
+        for (long z = z0; z <= z1; ++z) {
+            float p[3];
+            p[2] = centers[axis_offset(2) + uint32_t(z)];
+            for (uint32_t y = lo[1]; y <= hi[1]; ++y) {
+                p[1] = centers[axis_offset(1) + y];
+                uint8_t *row = &index_cache_[(uint64_t(z) * g.n[1] + y) * g.n[0]];
+                for (uint32_t x = lo[0]; x <= hi[0]; ++x) {
+                    p[0] = centers[x];
+                    if (shape_contains(sh, p)) row[x] = material;
+                }
+            }
+        }
+    }
+    indexed_ = true;
+    return index_cache_;
+}
 
 Scene Scene::build(const dp_scene_desc &d) {
     Scene s;
@@ -394,35 +436,6 @@ Scene Scene::build(const dp_scene_desc &d) {
     s.reversible = s.absorber_peak == 0.0f;
     for (const Coeff &c : s.coefficients)
         if (!(c.electric_loss == 0.0f && c.magnetic_loss == 0.0f)) s.reversible = false;
-
-    // Scene::material_indices, src/scene.rs:181-206: later shapes overwrite
-    // earlier ones, membership decided at the cell centre.
-    const uint64_t cells = g.cells();
-    s.material_index.assign(cells, 0);
-    for (const dp_shape &sh : s.shapes) {
-        uint32_t lo[3], hi[3];
-        bool empty = false;
-        for (int a = 0; a < 3; ++a) {
-            shape_range(g, sh, a, lo[a], hi[a]);
-            if (lo[a] > hi[a]) empty = true;
-        }
-        if (empty) continue;
-        const uint8_t material = uint8_t(sh.material);
-        const long z0 = lo[2], z1 = hi[2];
-#pragma omp parallel for schedule(dynamic, 1)
-        for (long z = z0; z <= z1; ++z) {
-            float p[3];
-            p[2] = s.centers[s.axis_offset(2) + uint32_t(z)];
-            for (uint32_t y = lo[1]; y <= hi[1]; ++y) {
-                p[1] = s.centers[s.axis_offset(1) + y];
-                uint8_t *row = &s.material_index[(uint64_t(z) * g.n[1] + y) * g.n[0]];
-                for (uint32_t x = lo[0]; x <= hi[0]; ++x) {
-                    p[0] = s.centers[x];
-                    if (shape_contains(sh, p)) row[x] = material;
-                }
-            }
-        }
-    }
 
     // Sheet apodization planes (src/source.rs:304-333 with the weight of
     // src/source.rs:441-455), evaluated once per sheet.

@@ -96,7 +96,6 @@ struct Scene {
     std::vector<float> dual;           // nx | ny | nz
     std::vector<float> absorber;       // integer x|y|z then half x|y|z
     std::vector<Coeff> coefficients;
-    std::vector<uint8_t> material_index;
     float absorber_peak = 0.0f;
     bool reversible = false;
     float dt = 0.0f;
@@ -107,7 +106,18 @@ struct Scene {
     std::vector<float> weights;
     std::vector<int32_t> source_weight;
 
+  private:
+    mutable std::vector<uint8_t> index_cache_;
+    mutable bool indexed_ = false;
+
+  public:
+
     static Scene build(const dp_scene_desc &desc);
+
+    // Scene::material_indices (src/scene.rs:181-206) on the host, computed on
+    // first use.  The simulation paths rasterize on the device instead
+    // (raster.cu); this copy serves the table export and host-side checks.
+    const std::vector<uint8_t> &material_index() const;
     uint32_t axis_offset(int axis) const { return axis == 0 ? 0 : (axis == 1 ? grid.n[0] : grid.n[0] + grid.n[1]); }
 
     // Source::injections for every source at `time`, two slots per source.
@@ -120,5 +130,11 @@ struct Scene {
 template <typename T> T waveform_in(const dp_waveform &w, T time);
 inline float waveform_value(const dp_waveform &w, float time) { return waveform_in<float>(w, time); }
 float injection_weight(const StepInjection &inj, const float position[3]);
+
+// Shape::contains, src/scene.rs:60-81: membership of a cell centre.
+bool shape_contains(const dp_shape &s, const float p[3]);
+// The cells along `axis` a shape can cover (a conservative range, widened by
+// two cells against rounding); lo > hi when it covers none.
+void shape_cell_range(const ResolvedGrid &g, const dp_shape &s, int axis, uint32_t &lo, uint32_t &hi);
 
 } // namespace diaphane

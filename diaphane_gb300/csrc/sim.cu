@@ -249,11 +249,10 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
     d.pitch = sim->pitch;
     d.cells = cells;
     {
-        std::vector<uint8_t> pitched(cells, 0);
-        const uint64_t rows = uint64_t(s.grid.n[1]) * s.grid.n[2];
-        for (uint64_t r = 0; r < rows; ++r)
-            std::memcpy(&pitched[r * sim->pitch], &s.material_index[r * nx], nx);
-        d.material = device_upload(pitched, owned, st);
+        // The index is rasterized on the device, straight into its buffer.
+        uint8_t *material = device_alloc<uint8_t>(cells, owned);
+        rasterize_on_device(s, material, sim->pitch, st);
+        d.material = material;
     }
     // Padded to all 256 u8 indices, so a kernel may stage the whole table.
     std::vector<float4> coeff(256, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
@@ -299,12 +298,10 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
             throw Error(DP_ERR_UNSUPPORTED, e.what());
         }
         // The index again with rows padded to 16 bytes, for its tensor map.
-        const uint32_t rows = s.grid.n[1] * s.grid.n[2];
+        const uint64_t rows = uint64_t(s.grid.n[1]) * s.grid.n[2];
         sim->material_pitch = (nx + 15) / 16 * 16;
-        std::vector<uint8_t> padded(size_t(sim->material_pitch) * rows, 0);
-        for (size_t r = 0; r < rows; ++r)
-            std::memcpy(&padded[r * sim->material_pitch], &s.material_index[r * nx], nx);
-        sim->material_padded = device_upload(padded, owned, st);
+        sim->material_padded = device_alloc<uint8_t>(size_t(sim->material_pitch) * rows, owned);
+        rasterize_on_device(s, sim->material_padded, sim->material_pitch, st);
         check(cudaStreamSynchronize(st), "setup upload");
         try {
             for (int k = 0; k < 2; ++k)

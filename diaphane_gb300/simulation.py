@@ -64,6 +64,11 @@ class ResolvedScene:
             _abi.lib().dp_scene_destroy(self.handle)
             self.handle = None
 
+    def rasterize(self, device_ptr: int, row_pitch: int = 0, stream: int = 0) -> None:
+        """The material index rasterized on the GPU into device memory at
+        `device_ptr` (rows of `row_pitch` bytes, 0 = nx), on `stream`."""
+        _abi.check(_abi.lib().dp_scene_raster(self.handle, C.c_void_p(device_ptr), row_pitch, C.c_void_p(stream)))
+
     def table(self, which: int) -> np.ndarray:
         span = sum(self.extent)
         sizes = {
