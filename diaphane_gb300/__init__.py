@@ -9,10 +9,10 @@ from .scene import (Axis, Boundary, Extent, Grid, Material, MaterialTable, Refin
                     Waveform, COURANT_LIMIT, SPEED_OF_LIGHT)
 from .simulation import Energy, ResolvedScene, Simulation, Simulation64, Snapshot
 from .batch import Batch
-from .timeline import Seek, Timeline
+from .timeline import DeviceTimeline, Seek, Timeline
 
 __all__ = [
-    "Axis", "Batch", "Boundary", "COURANT_LIMIT", "DiaphaneError", "DP_KERNEL_AUTO", "DP_KERNEL_FUSED", "DP_KERNEL_NAIVE",
+    "Axis", "Batch", "DeviceTimeline", "Boundary", "COURANT_LIMIT", "DiaphaneError", "DP_KERNEL_AUTO", "DP_KERNEL_FUSED", "DP_KERNEL_NAIVE",
     "Energy", "Extent", "Grid", "Material", "MaterialTable", "Refinement", "ResolvedScene", "Scene", "Seek",
     "Shape", "Simulation", "Simulation64", "Snapshot", "SPEED_OF_LIGHT", "Source", "Timeline", "Waveform",
 ]

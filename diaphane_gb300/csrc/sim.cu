@@ -4,17 +4,7 @@
 // The fused step reads one set and writes the other (ping-pong), which is
 // what lets H and E of a whole step be computed in a single pass over HBM.
 // The naive passes and the reverse step work in place on the current set.
-#include "abi.hpp"
-#include "device.cuh"
-
-#include <chrono>
-#include <cstring>
-#include <thread>
-#include <vector>
-
-namespace diaphane {
-const Scene &scene_of(const dp_scene *s);
-}
+#include "sim.hpp"
 
 using namespace diaphane;
 
@@ -45,173 +35,24 @@ template <typename T> T *device_upload(const std::vector<T> &host, std::vector<v
 
 } // namespace
 
-struct dp_sim {
-    Scene scene;
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    uint32_t kernel = DP_KERNEL_NAIVE;
-    DeviceScene dev{};
-    FieldSet set[2]{};
-    int current = 0;
-    float *intensity = nullptr;
-    float *primary = nullptr;
-    float *dual = nullptr;
-    float2 *eps_mu = nullptr;
-    double *partials = nullptr;
-    double *host_partials = nullptr;
-    int32_t *flag = nullptr;
-    int32_t *error = nullptr;        // set by a kernel whose bounded wait gave up
-    uint8_t *material_padded = nullptr;
-    uint32_t material_pitch = 0;
-    uint32_t pitch = 0;              // field row stride in cells (nx rounded up to 4)
-    FusedPlan plan{};
-    FusedMaps maps[2]{};             // tensor maps reading set 0 / set 1
-    std::vector<void *> owned;
-    uint64_t step = 0;
-    uint64_t accumulated = 0;
-    bool accumulating = false;
-    uint64_t launches = 0;
-    std::vector<StepInjection> injections;
+namespace {
 
-    ~dp_sim() {
-        if (stream) {
-            cudaSetDevice(device);
-            cudaStreamSynchronize(stream);
-        }
-        for (void *p : owned) cudaFree(p);
-        if (host_partials) cudaFreeHost(host_partials);
-        if (stream) cudaStreamDestroy(stream);
-    }
+__global__ void probe_gather(const float *e, const float *h, uint64_t cells, const uint32_t *probe_cells, uint32_t count,
+                             float *ring, uint64_t slot) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= count) return;
+    const uint64_t cell = probe_cells[k];
+    float *record = ring + (slot * count + k) * 2;
+    record[0] = e[2 * cells + cell]; // Ez
+    record[1] = h[cells + cell];     // Hy
+}
 
-    void bind() { check(cudaSetDevice(device), "cudaSetDevice"); }
+} // namespace
 
-    FieldSet fields() const { return set[current]; }
-
-    // The non-silent injections of one phase at `time`, in application order
-    // (apply_sources, src/cpu.rs:606-633).
-    void collect(float time, std::vector<DeviceInjection> &out) {
-        out.clear();
-        scene.injections(time, injections);
-        for (const StepInjection &s : injections) {
-            if (s.value == 0.0f) continue;
-            DeviceInjection d{};
-            for (int a = 0; a < 3; ++a) {
-                d.origin[a] = s.origin[a];
-                d.extent[a] = s.extent[a];
-            }
-            d.component = s.component;
-            d.magnetic = s.magnetic;
-            d.value = s.value;
-            d.weight_offset = s.weight_offset;
-            out.push_back(d);
-        }
-    }
-
-    void inject_phase(const std::vector<DeviceInjection> &all, bool magnetic, float sign) {
-        for (const DeviceInjection &d : all) {
-            if (bool(d.magnetic) != magnetic) continue;
-            launch_inject(dev, fields(), d, sign, stream);
-            ++launches;
-        }
-    }
-
-    // advance (src/cpu.rs:174-198, src/gpu.rs:425-481).
-    void forward(uint64_t steps) {
-        std::vector<DeviceInjection> all;
-        for (uint64_t n = 0; n < steps; ++n) {
-            // `E` holds (step + 1)·dt after its update; injections are stated
-            // relative to that instant.
-            const float time = float(step + 1) * scene.dt;
-            collect(time, all);
-            if (kernel == DP_KERNEL_FUSED) {
-                InjectionTable table{};
-                table.count = uint32_t(all.size());
-                for (size_t k = 0; k < all.size(); ++k) table.item[k] = all[k];
-                launch_fused_step(dev, plan, maps[current], set[current ^ 1], accumulating ? intensity : nullptr,
-                                  table, error, stream);
-                ++launches;
-                current ^= 1;
-            } else {
-                launch_naive_magnetic(dev, fields(), false, stream);
-                ++launches;
-                inject_phase(all, true, 1.0f);
-                launch_naive_electric(dev, fields(), false, stream);
-                ++launches;
-                inject_phase(all, false, 1.0f);
-                if (accumulating) {
-                    launch_intensity(dev, fields().e, intensity, stream);
-                    ++launches;
-                }
-            }
-            check(cudaGetLastError(), "step launch");
-            if (accumulating) ++accumulated;
-            ++step;
-        }
-    }
-
-    // reverse (src/cpu.rs:253-273, src/gpu.rs:537-573): each forward phase
-    // undone in the opposite order with the drive negated.
-    void backward(uint64_t steps) {
-        std::vector<DeviceInjection> all;
-        for (uint64_t n = 0; n < steps; ++n) {
-            const float time = float(step) * scene.dt;
-            collect(time, all);
-            inject_phase(all, false, -1.0f);
-            launch_naive_electric(dev, fields(), true, stream);
-            ++launches;
-            inject_phase(all, true, -1.0f);
-            launch_naive_magnetic(dev, fields(), true, stream);
-            ++launches;
-            check(cudaGetLastError(), "reverse launch");
-            --step;
-        }
-    }
-
-    uint64_t padded_cells() const { return uint64_t(pitch) * scene.grid.n[1] * scene.grid.n[2]; }
-
-    void clear_intensity() {
-        if (accumulated == 0) return;
-        check(cudaMemsetAsync(intensity, 0, padded_cells() * sizeof(float), stream), "clear intensity");
-        accumulated = 0;
-    }
-
-    // Dense host rows <-> pitched device rows, `components` of them.
-    void copy_out(float *host, const float *device, int components) {
-        const uint32_t *n = scene.grid.n;
-        const uint64_t dense = scene.grid.cells(), padded = padded_cells();
-        for (int c = 0; c < components; ++c)
-            check(cudaMemcpy2DAsync(host + c * dense, size_t(n[0]) * 4, device + c * padded, size_t(pitch) * 4,
-                                    size_t(n[0]) * 4, size_t(n[1]) * n[2], cudaMemcpyDeviceToHost, stream),
-                  "readback");
-    }
-    void copy_in(float *device, const float *host, int components) {
-        const uint32_t *n = scene.grid.n;
-        const uint64_t dense = scene.grid.cells(), padded = padded_cells();
-        for (int c = 0; c < components; ++c)
-            check(cudaMemcpy2DAsync(device + c * padded, size_t(pitch) * 4, host + c * dense, size_t(n[0]) * 4,
-                                    size_t(n[0]) * 4, size_t(n[1]) * n[2], cudaMemcpyHostToDevice, stream),
-                  "upload");
-    }
-
-    void wait(uint32_t timeout_ms) {
-        const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
-        for (;;) {
-            cudaError_t q = cudaStreamQuery(stream);
-            if (q == cudaSuccess) break;
-            if (q != cudaErrorNotReady) check(q, "stream");
-            if (std::chrono::steady_clock::now() >= deadline) throw Error(DP_ERR_TIMEOUT, "the GPU did not finish in time");
-            std::this_thread::sleep_for(std::chrono::microseconds(50));
-        }
-        if (kernel == DP_KERNEL_FUSED) {
-            int32_t code = 0;
-            check(cudaMemcpy(&code, error, sizeof(code), cudaMemcpyDeviceToHost), "error flag");
-            if (code != 0) {
-                check(cudaMemset(error, 0, sizeof(int32_t)), "error flag");
-                throw Error(DP_ERR_TIMEOUT, "a fused step gave up waiting for its plane loads");
-            }
-        }
-    }
-};
+void diaphane::launch_probe_gather(const float *e, const float *h, uint64_t cells, const uint32_t *probe_cells,
+                                   uint32_t count, float *ring, uint64_t slot, cudaStream_t stream) {
+    probe_gather<<<(count + 127) / 128, 128, 0, stream>>>(e, h, cells, probe_cells, count, ring, slot);
+}
 
 namespace {
 
@@ -371,15 +212,7 @@ dp_status dp_sim_reset(dp_sim *sim) {
     return guarded([&] {
         if (!sim) throw Error(DP_ERR_INVALID, "null handle");
         sim->bind();
-        const uint64_t cells = sim->padded_cells();
-        for (int k = 0; k < 2; ++k) {
-            check(cudaMemsetAsync(sim->set[k].e, 0, 3 * cells * sizeof(float), sim->stream), "reset");
-            check(cudaMemsetAsync(sim->set[k].h, 0, 3 * cells * sizeof(float), sim->stream), "reset");
-        }
-        check(cudaMemsetAsync(sim->intensity, 0, cells * sizeof(float), sim->stream), "reset");
-        sim->current = 0;
-        sim->step = 0;
-        sim->accumulated = 0;
+        sim->reset_fields();
         return DP_OK;
     });
 }
@@ -417,6 +250,7 @@ dp_status dp_sim_write_field(dp_sim *sim, uint32_t field, const float *host, siz
         sim->wait(kDefaultTimeoutMs);
         sim->copy_in(field_ptr(sim, field), host, field == DP_FIELD_INTENSITY ? 1 : 3);
         sim->wait(kDefaultTimeoutMs);
+        if (field != DP_FIELD_INTENSITY) sim->probe_since = sim->step;
         return DP_OK;
     });
 }
@@ -433,6 +267,7 @@ dp_status dp_sim_restore(dp_sim *sim, uint64_t step, const float *electric, cons
         sim->copy_in(sim->fields().h, magnetic, 3);
         sim->wait(kDefaultTimeoutMs);
         sim->step = step;
+        sim->probe_since = step;
         return DP_OK;
     });
 }
@@ -516,5 +351,75 @@ uint32_t dp_sim_kernel(const dp_sim *sim) { return sim ? sim->kernel : 0; }
 uint32_t dp_sim_row_pitch(const dp_sim *sim) { return sim ? sim->pitch : 0; }
 
 uint64_t dp_sim_launch_count(const dp_sim *sim) { return sim ? sim->launches : 0; }
+
+dp_status dp_sim_read_field_async(dp_sim *sim, uint32_t field, float *host, size_t count) {
+    return guarded([&] {
+        if (!sim || !host) throw Error(DP_ERR_INVALID, "null argument");
+        if (count != field_count(sim, field)) throw Error(DP_ERR_RANGE, "element count does not match the field");
+        sim->bind();
+        sim->copy_out(host, field_ptr(sim, field), field == DP_FIELD_INTENSITY ? 1 : 3);
+        return DP_OK;
+    });
+}
+
+dp_status dp_sim_set_probes(dp_sim *sim, const uint32_t *cells, uint32_t count, uint64_t capacity) {
+    return guarded([&] {
+        if (!sim || (count && !cells)) throw Error(DP_ERR_INVALID, "null argument");
+        if (count && capacity == 0) throw Error(DP_ERR_INVALID, "a probe ring needs room for at least one step");
+        const uint32_t *n = sim->scene.grid.n;
+        std::vector<uint32_t> padded(count);
+        for (uint32_t k = 0; k < count; ++k) {
+            const uint32_t *c = cells + 3 * k;
+            if (c[0] >= n[0] || c[1] >= n[1] || c[2] >= n[2]) throw Error(DP_ERR_RANGE, "probe outside the grid");
+            const uint64_t index = (uint64_t(c[2]) * n[1] + c[1]) * sim->pitch + c[0];
+            if (index > 0xffffffffull) throw Error(DP_ERR_RANGE, "probe index beyond 32 bits");
+            padded[k] = uint32_t(index);
+        }
+        sim->bind();
+        sim->wait(kDefaultTimeoutMs); // the old ring may still be written
+        cudaFree(sim->probe_cells);
+        cudaFree(sim->probe_ring);
+        sim->probe_cells = nullptr;
+        sim->probe_ring = nullptr;
+        sim->probe_count = 0;
+        sim->probe_capacity = 0;
+        if (count == 0) return DP_OK;
+        check(cudaMalloc(&sim->probe_cells, count * sizeof(uint32_t)), "probe cells");
+        check(cudaMalloc(&sim->probe_ring, size_t(capacity) * count * 2 * sizeof(float)), "probe ring");
+        check(cudaMemcpy(sim->probe_cells, padded.data(), count * sizeof(uint32_t), cudaMemcpyHostToDevice), "probes");
+        sim->probe_count = count;
+        sim->probe_capacity = capacity;
+        sim->probe_since = sim->step;
+        return DP_OK;
+    });
+}
+
+dp_status dp_sim_read_probes(dp_sim *sim, uint64_t first_step, uint64_t steps, float *host, size_t count) {
+    return guarded([&] {
+        if (!sim || (steps && !host)) throw Error(DP_ERR_INVALID, "null argument");
+        if (count != steps * sim->probe_count * 2) throw Error(DP_ERR_RANGE, "element count does not match the window");
+        if (steps == 0) return DP_OK;
+        const uint64_t last = first_step + steps - 1;
+        const uint64_t oldest = std::max(sim->probe_since + 1, sim->step >= sim->probe_capacity
+                                                                   ? sim->step - sim->probe_capacity + 1
+                                                                   : uint64_t(1));
+        if (first_step < oldest || last > sim->step)
+            throw Error(DP_ERR_RANGE, "those steps are not in the probe ring");
+        sim->bind();
+        sim->wait(kDefaultTimeoutMs);
+        const size_t record = size_t(sim->probe_count) * 2;
+        uint64_t s = first_step;
+        float *out = host;
+        while (s <= last) {
+            const uint64_t slot = (s - 1) % sim->probe_capacity;
+            const uint64_t run = std::min(last - s + 1, sim->probe_capacity - slot);
+            check(cudaMemcpy(out, sim->probe_ring + slot * record, run * record * sizeof(float), cudaMemcpyDeviceToHost),
+                  "probe readback");
+            out += run * record;
+            s += run;
+        }
+        return DP_OK;
+    });
+}
 
 } // extern "C"

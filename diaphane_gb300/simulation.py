@@ -209,6 +209,26 @@ class Simulation:
     def snapshot(self) -> Snapshot:
         return Snapshot(self.step_count(), self.read_electric(), self.read_magnetic())
 
+    # -- probes and asynchronous read-back ---------------------------------------
+    def set_probes(self, cells, capacity: int) -> None:
+        """Ez and Hy at `cells` ((x, y, z) each) after every step, kept for the
+        last `capacity` steps in device memory; no cells removes them."""
+        flat = (C.c_uint32 * max(1, 3 * len(cells)))(*[int(v) for c in cells for v in c])
+        _abi.check(_abi.lib().dp_sim_set_probes(self.handle, flat, len(cells), capacity))
+        self.probe_count = len(cells)
+
+    def read_probes(self, first_step: int, steps: int) -> np.ndarray:
+        """steps × probes × (Ez, Hy) for steps first_step .. first_step+steps-1."""
+        count = steps * self.probe_count * 2
+        out = np.empty(max(count, 1), dtype=np.float32)
+        _abi.check(_abi.lib().dp_sim_read_probes(self.handle, first_step, steps, out.ctypes.data, count))
+        return out[:count].reshape(steps, self.probe_count, 2)
+
+    def read_field_async(self, field: int, host_ptr: int, count: int) -> None:
+        """Queues a read of `field` into host memory at `host_ptr` (pinned for
+        overlap); the data is there after wait()."""
+        _abi.check(_abi.lib().dp_sim_read_field_async(self.handle, field, C.c_void_p(host_ptr), count))
+
     def restore(self, snapshot: Snapshot) -> None:
         e = np.ascontiguousarray(snapshot.electric, dtype=np.float32)
         h = np.ascontiguousarray(snapshot.magnetic, dtype=np.float32)
