@@ -97,6 +97,22 @@ class dp_options(C.Structure):
 
 # Every entry point declared in include/diaphane_gb300.h: (name, restype, argtypes).
 _P = C.c_void_p
+class dp_view(C.Structure):
+    _fields_ = [("yaw", C.c_float), ("pitch", C.c_float), ("distance", C.c_float), ("fov", C.c_float),
+                ("mode", C.c_uint32), ("gain", C.c_float), ("log_strength", C.c_float), ("scrub", C.c_int32),
+                ("played", C.c_float), ("window_start", C.c_float)]
+
+
+DP_VIEW_ENERGY, DP_VIEW_ELECTRIC, DP_VIEW_MAGNETIC, DP_VIEW_MAGNITUDE = 0, 1, 2, 3
+DP_VIEW_FIELDS, DP_VIEW_GRID, DP_VIEW_RIBBONS, DP_VIEW_INTENSITY = 4, 5, 6, 7
+
+
+class dp_seek(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("replayed", C.c_uint64), ("at", C.c_uint64)]
+
+
+DP_SEEK_UNCHANGED, DP_SEEK_FORWARD, DP_SEEK_KEYFRAME, DP_SEEK_START = 0, 1, 2, 3
+
 SIGNATURES = [
     ("dp_last_error", C.c_char_p, []),
     ("dp_status_string", C.c_char_p, [C.c_int]),
@@ -145,6 +161,25 @@ SIGNATURES = [
     ("dp_sim_row_pitch", C.c_uint32, [_P]),
     ("dp_sim_launch_count", C.c_uint64, [_P]),
     ("dp_scene_raster", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("dp_sim_set_probes", C.c_int, [_P, _P, C.c_uint32, C.c_uint64]),
+    ("dp_sim_read_probes", C.c_int, [_P, C.c_uint64, C.c_uint64, _P, C.c_size_t]),
+    ("dp_sim_read_field_async", C.c_int, [_P, C.c_uint32, _P, C.c_size_t]),
+    ("dp_keyframes_create", C.c_int, [_P, C.c_uint64, C.c_uint32, C.POINTER(_P)]),
+    ("dp_keyframes_destroy", None, [_P]),
+    ("dp_keyframes_observe", C.c_int, [_P]),
+    ("dp_keyframes_seek", C.c_int, [_P, C.c_uint64, C.POINTER(dp_seek)]),
+    ("dp_keyframes_clear", C.c_int, [_P]),
+    ("dp_keyframes_count", C.c_uint32, [_P]),
+    ("dp_keyframes_earliest", C.c_int, [_P, C.POINTER(C.c_uint64)]),
+    ("dp_keyframes_bytes", C.c_uint64, [_P]),
+    ("dp_view_default", dp_view, []),
+    ("dp_renderer_create", C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(_P)]),
+    ("dp_renderer_destroy", None, [_P]),
+    ("dp_renderer_measure", C.c_int, [_P]),
+    ("dp_renderer_draw", C.c_int, [_P, C.POINTER(dp_view), C.c_int32]),
+    ("dp_renderer_pixels", C.c_int, [_P, _P, C.c_size_t]),
+    ("dp_renderer_image", C.c_int, [_P, C.POINTER(_P)]),
+    ("dp_renderer_state", C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_uint32)]),
     ("dp_sim64_create", C.c_int, [_P, C.c_int32, C.POINTER(_P)]),
     ("dp_sim64_destroy", None, [_P]),
     ("dp_sim64_advance", C.c_int, [_P, C.c_uint64]),

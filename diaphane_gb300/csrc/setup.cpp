@@ -172,6 +172,7 @@ ResolvedGrid ResolvedGrid::build(const dp_grid_spec &spec) {
         g.n[a] = uint32_t(g.axes[a].primary.size());
     }
     g.courant = spec.courant;
+    g.base = spec.cell_size;
     return g;
 }
 

@@ -48,6 +48,7 @@ Axis1D axis_graded(int axis, float length, float base, const dp_refinement *refi
 struct ResolvedGrid {
     uint32_t n[3];
     float courant;
+    float base; // the base (coarse) cell size, metres
     Axis1D axes[3];
 
     static ResolvedGrid build(const dp_grid_spec &spec);

@@ -363,6 +363,95 @@ uint32_t dp_sim_kernel(const dp_sim *sim);
 /* Kernel launches issued by this handle so far (every kernel of this library). */
 uint64_t dp_sim_launch_count(const dp_sim *sim);
 
+/* ---- Probes and asynchronous read-back ----------------------------------
+ * Probes record Ez and Hy at given cells after every step into a device ring
+ * of `capacity` steps (one small gather launch per step while set); count 0
+ * removes them.  A restore, reset or field write starts a new history, and
+ * only steps recorded since are readable. */
+dp_status dp_sim_set_probes(dp_sim *sim, const uint32_t *cells_xyz, uint32_t count, uint64_t capacity);
+/* Steps first_step .. first_step+steps-1 (step k = the state after k steps),
+ * steps × probes × (Ez, Hy) floats; DP_ERR_RANGE outside the ring. */
+dp_status dp_sim_read_probes(dp_sim *sim, uint64_t first_step, uint64_t steps, float *host, size_t count);
+/* dp_sim_read_field without the wait: the copy is queued on the handle's
+ * stream behind the steps already issued; the host buffer (pinned for true
+ * overlap) is valid after dp_sim_wait. */
+dp_status dp_sim_read_field_async(dp_sim *sim, uint32_t field, float *host, size_t count);
+
+/* ---- Device keyframes (Timeline, src/timeline.rs:76-213) -----------------
+ * A ring of `capacity` field snapshots kept in device memory (24 bytes per
+ * cell each, allocated at creation) for a simulation that must outlive it.
+ * observe records a keyframe when the step has crossed into a later interval
+ * than the newest one; seek goes to a step by the cheapest route: forward by
+ * stepping, backward by restoring the newest keyframe at or before it and
+ * replaying, or from a reset when the window has slid past it.  Snapshots and
+ * restores are device-to-device copies on the simulation's stream. */
+typedef struct dp_keyframes dp_keyframes;
+enum { DP_SEEK_UNCHANGED = 0, DP_SEEK_FORWARD = 1, DP_SEEK_KEYFRAME = 2, DP_SEEK_START = 3 };
+/* Seek (src/timeline.rs:83-106): what a seek had to do. */
+typedef struct dp_seek {
+    uint32_t kind;     /* DP_SEEK_* */
+    uint64_t replayed; /* steps run */
+    uint64_t at;       /* the keyframe restored (DP_SEEK_KEYFRAME) */
+} dp_seek;
+dp_status dp_keyframes_create(dp_sim *sim, uint64_t interval, uint32_t capacity, dp_keyframes **out);
+void dp_keyframes_destroy(dp_keyframes *keyframes);
+dp_status dp_keyframes_observe(dp_keyframes *keyframes);
+dp_status dp_keyframes_seek(dp_keyframes *keyframes, uint64_t target, dp_seek *out);
+dp_status dp_keyframes_clear(dp_keyframes *keyframes);
+uint32_t dp_keyframes_count(const dp_keyframes *keyframes);
+dp_status dp_keyframes_earliest(const dp_keyframes *keyframes, uint64_t *step);
+/* Bytes the recorded keyframes stand for, 24 per cell each (Timeline::bytes). */
+uint64_t dp_keyframes_bytes(const dp_keyframes *keyframes);
+
+/* ---- Headless volume renderer -------------------------------------------
+ * The reference viewer's volume pass (examples/common/shaders/volume.wgsl)
+ * and exposure control (examples/common/render.rs) on a simulation's own
+ * device buffers, into an RGBA8 image (sRGB-encoded, row 0 at the top) in
+ * device memory.  No window, swapchain or graphics API: the image can be
+ * read back or used in place.  The renderer borrows the simulation, which
+ * must outlive it; work is queued on the simulation's stream. */
+typedef struct dp_renderer dp_renderer;
+/* ViewMode (render.rs:12-47), with the shader's mode codes. */
+enum {
+    DP_VIEW_ENERGY = 0,
+    DP_VIEW_ELECTRIC = 1,
+    DP_VIEW_MAGNETIC = 2,
+    DP_VIEW_MAGNITUDE = 3,
+    DP_VIEW_FIELDS = 4,
+    DP_VIEW_GRID = 5,
+    DP_VIEW_RIBBONS = 6,
+    DP_VIEW_INTENSITY = 7
+};
+/* Camera (examples/common/camera.rs) and ViewSettings (render.rs:118-137). */
+typedef struct dp_view {
+    float yaw, pitch;   /* orbit angles, radians */
+    float distance;     /* from the box centre, in longest sides */
+    float fov;          /* vertical field of view, radians */
+    uint32_t mode;      /* DP_VIEW_* */
+    float gain;         /* multiplies the auto-ranged exposure */
+    float log_strength; /* signed-log compression, 0 = linear */
+    int32_t scrub;      /* nonzero: draw the scrub bar */
+    float played;       /* scrub bar playhead, 0..1 */
+    float window_start; /* start of the keyframed window, 0..1 */
+} dp_view;
+/* Camera::new and ViewSettings::new: yaw 0.9, pitch 0.45, distance 1.9,
+ * fov 0.8, the E-and-H view, gain 1, log strength 6, no scrub bar. */
+dp_view dp_view_default(void);
+dp_status dp_renderer_create(dp_sim *sim, uint32_t width, uint32_t height, dp_renderer **out);
+void dp_renderer_destroy(dp_renderer *renderer);
+/* The peak reduction on its own (Renderer::measure): run once before the
+ * first draw, whose exposure comes from the previous reduction. */
+dp_status dp_renderer_measure(dp_renderer *renderer);
+/* Renderer::draw: folds the previous reduction into the exposure (only when
+ * `advanced`), reduces again, and ray-marches the frame. */
+dp_status dp_renderer_draw(dp_renderer *renderer, const dp_view *view, int32_t advanced);
+dp_status dp_renderer_pixels(dp_renderer *renderer, uint8_t *host_rgba, size_t bytes);
+dp_status dp_renderer_image(dp_renderer *renderer, void **device_rgba);
+/* The last reduction's eight slots (energy-density peak, |E| and |H| per
+ * component, averaged intensity), the exposure scale, and the components of
+ * E and H the signed views read; any pointer may be null. */
+dp_status dp_renderer_state(dp_renderer *renderer, float peaks[8], float *scale, uint32_t components[2]);
+
 /* ---- FP64 instance ------------------------------------------------------
  * The same time step in double on the GPU: fields, curls, updates, drive
  * values and time in f64 over the f32 setup tables, i.e. the reference's
