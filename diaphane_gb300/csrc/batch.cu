@@ -93,9 +93,10 @@ struct Variant {
     bool operator==(const Variant &o) const { return cx == o.cx && tile_y == o.tile_y && slots == o.slots; }
 };
 
-// The variant a grid shape runs: the widest tile that wastes no more lanes
-// than a narrower one, 8 rows, and the ring depth that variant is built with.
-Variant variant_for(uint32_t nx) {
+// The variant a grid shape runs: the requested tile width, or else the widest
+// tile that wastes no more lanes than a narrower one; 8 rows, and the ring
+// depth that variant is built with.
+Variant variant_for(uint32_t nx, uint32_t requested_cx) {
     uint32_t best = 4, waste_best = ~0u;
     for (uint32_t cx : {4u, 2u, 1u}) {
         const uint32_t tx = 32 * cx, waste = (nx + tx - 1) / tx * tx - nx;
@@ -104,6 +105,7 @@ Variant variant_for(uint32_t nx) {
             waste_best = waste;
         }
     }
+    if (requested_cx) best = requested_cx;
     return Variant{best, 8, best == 4 ? 3u : 5u};
 }
 
@@ -155,6 +157,7 @@ struct dp_batch {
     cudaStream_t stream = nullptr;
     uint32_t chunk = 50;
     uint32_t capacity = 0;        // scene slots
+    uint32_t cells_per_lane = 0;  // forced tile width (0: per scene)
     bool graphs = true;
     unsigned char *arena_base = nullptr;
     Arena arena;
@@ -431,6 +434,10 @@ dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out) {
         b->chunk = opts->chunk_steps ? opts->chunk_steps : 50;
         b->capacity = opts->max_scenes ? opts->max_scenes : 256;
         b->graphs = opts->use_graphs != 0;
+        if (opts->cells_per_lane != 0 && opts->cells_per_lane != 1 && opts->cells_per_lane != 2 &&
+            opts->cells_per_lane != 4)
+            throw Error(DP_ERR_INVALID, "cells_per_lane must be 0, 1, 2 or 4");
+        b->cells_per_lane = opts->cells_per_lane;
         if (opts->arena_bytes == 0) throw Error(DP_ERR_INVALID, "arena_bytes must be positive");
         b->bind();
         check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
@@ -479,7 +486,7 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         e.id = b->next_id++;
         e.scene = s;
         e.slot = slot;
-        e.variant = variant_for(s.grid.n[0]);
+        e.variant = variant_for(s.grid.n[0], b->cells_per_lane);
         e.pitch = l.pitch;
         e.material_pitch = l.material_pitch;
         e.cells_padded = l.cells;

@@ -451,6 +451,9 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         // Material coefficients of this lane's cells, kept for the E phase.
         float2 ecoef[CX]; // (electric_gain, electric_loss)
 
+        // New H at this thread's cells, kept in registers for the E phase
+        // (the other warps read it from the H slot).
+        Vec<CX> kept_hx, kept_hy, kept_hz;
         // ---------------- H(p): this warp's row ----------------
         {
             const Vec<CX> ex = lds<CX>(e_at(E, 0, row, col)), ex_up = lds<CX>(e_at(E, 0, row + 1, col));
@@ -533,6 +536,9 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 hx_prev = nhx;
                 hy_prev = nhy;
             } else {
+                kept_hx = nhx;
+                kept_hy = nhy;
+                kept_hz = nhz;
                 sts<CX>(h_at(H, 0, row, col), nhx);
                 sts<CX>(h_at(H, 1, row, col), nhy);
                 sts<CX>(h_at(H, 2, row, col), nhz);
@@ -565,8 +571,7 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
 
         // ---------------- E(p) ----------------
         {
-            const Vec<CX> hx = lds<CX>(h_at(H, 0, row, col)), hy = lds<CX>(h_at(H, 1, row, col));
-            const Vec<CX> hz = lds<CX>(h_at(H, 2, row, col));
+            const Vec<CX> hx = kept_hx, hy = kept_hy, hz = kept_hz;
             const Vec<CX> hx_dn = lds<CX>(h_at(H, 0, row - 1, col)), hz_dn = lds<CX>(h_at(H, 2, row - 1, col));
             float hy_left = __shfl_up_sync(0xffffffffu, hy.v[CX - 1], 1);
             float hz_left = __shfl_up_sync(0xffffffffu, hz.v[CX - 1], 1);
