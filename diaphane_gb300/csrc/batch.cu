@@ -528,7 +528,8 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         check(cudaMemcpyAsync(absorber, s.absorber.data(), s.absorber.size() * 4, cudaMemcpyHostToDevice, st), "absorber");
         if (!s.weights.empty())
             check(cudaMemcpyAsync(weights, s.weights.data(), s.weights.size() * 4, cudaMemcpyHostToDevice, st), "weights");
-        check(cudaStreamSynchronize(st), "scene upload");
+        // No wait: copies from pageable memory return once staged, and every
+        // later use of these buffers is ordered behind them on the stream.
         for (int a = 0; a < 3; ++a) d.s.n[a] = s.grid.n[a];
         d.s.pitch = l.pitch;
         d.s.cells = l.cells;
@@ -628,10 +629,11 @@ dp_status dp_batch_read_field(dp_batch *b, uint64_t id, uint32_t field, float *h
         const float *src = field == DP_FIELD_ELECTRIC ? e.desc.e[current]
                            : field == DP_FIELD_MAGNETIC ? e.desc.h[current] : e.desc.intensity;
         if (field > DP_FIELD_INTENSITY) throw Error(DP_ERR_INVALID, "unknown field");
-        for (int c = 0; c < components; ++c)
-            check(cudaMemcpy2DAsync(host + c * cells, size_t(n[0]) * 4, src + c * e.cells_padded, size_t(e.pitch) * 4,
-                                    size_t(n[0]) * 4, size_t(n[1]) * n[2], cudaMemcpyDeviceToHost, b->stream),
-                  "readback");
+        try {
+            copy_fields_out(host, src, n, e.pitch, e.cells_padded, components, b->stream);
+        } catch (const std::runtime_error &ex) {
+            throw Error(DP_ERR_CUDA, ex.what());
+        }
         b->wait(kTimeoutMs);
         return DP_OK;
     });

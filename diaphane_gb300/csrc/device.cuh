@@ -62,6 +62,20 @@ void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj,
 void launch_inject(const DeviceScene &s, FieldSet64 f, const DeviceInjection &inj, double value, cudaStream_t stream);
 void launch_intensity(const DeviceScene &s, const float *e, float *intensity, cudaStream_t stream);
 
+// Dense <-> pitched rows of `components` fields of `rows` rows each (pitch.cu).
+void launch_pack_rows(const float *src, float *dst, uint32_t nx, uint32_t pitch, uint64_t rows, uint64_t src_stride,
+                      uint32_t components, cudaStream_t stream);
+void launch_unpack_rows(const float *src, float *dst, uint32_t nx, uint32_t pitch, uint64_t rows, uint64_t dst_stride,
+                        uint32_t components, cudaStream_t stream);
+
+// Copies `components` pitched device fields (component stride `stride`) to or
+// from dense host rows: one contiguous transfer, packed on the device when the
+// pitch differs from nx.  Asynchronous on `stream`.
+void copy_fields_out(float *host, const float *device, const uint32_t n[3], uint32_t pitch, uint64_t stride,
+                     int components, cudaStream_t stream);
+void copy_fields_in(float *device, const float *host, const uint32_t n[3], uint32_t pitch, uint64_t stride,
+                    int components, cudaStream_t stream);
+
 // Scene::material_indices on the device (raster.cu): the u8 index with rows of
 // `pitch` bytes (padding cells 0), asynchronous on `stream`.
 struct Scene;

@@ -197,20 +197,18 @@ struct dp_sim {
 
     // Dense host rows <-> pitched device rows, `components` of them.
     void copy_out(float *host, const float *device, int components) {
-        const uint32_t *n = scene.grid.n;
-        const uint64_t dense = scene.grid.cells(), padded = padded_cells();
-        for (int c = 0; c < components; ++c)
-            diaphane::check_cuda(cudaMemcpy2DAsync(host + c * dense, size_t(n[0]) * 4, device + c * padded, size_t(pitch) * 4,
-                                    size_t(n[0]) * 4, size_t(n[1]) * n[2], cudaMemcpyDeviceToHost, stream),
-                  "readback");
+        try {
+            copy_fields_out(host, device, scene.grid.n, pitch, padded_cells(), components, stream);
+        } catch (const std::runtime_error &e) {
+            throw Error(DP_ERR_CUDA, e.what());
+        }
     }
     void copy_in(float *device, const float *host, int components) {
-        const uint32_t *n = scene.grid.n;
-        const uint64_t dense = scene.grid.cells(), padded = padded_cells();
-        for (int c = 0; c < components; ++c)
-            diaphane::check_cuda(cudaMemcpy2DAsync(device + c * padded, size_t(pitch) * 4, host + c * dense, size_t(n[0]) * 4,
-                                    size_t(n[0]) * 4, size_t(n[1]) * n[2], cudaMemcpyHostToDevice, stream),
-                  "upload");
+        try {
+            copy_fields_in(device, host, scene.grid.n, pitch, padded_cells(), components, stream);
+        } catch (const std::runtime_error &e) {
+            throw Error(DP_ERR_CUDA, e.what());
+        }
     }
 
     void wait(uint32_t timeout_ms) {
