@@ -59,6 +59,7 @@ def parse():
     p.add_argument("--batch-steps", type=int, default=1000, help="batched: steps per scene")
     p.add_argument("--rates", default="4,16,64", help="served: arrival rates to sweep, requests/s")
     p.add_argument("--requests", type=int, default=48, help="served: requests per trace")
+    p.add_argument("--ref-budget", type=float, default=60.0, help="reference arm: seconds of CPU stepping")
     return p.parse_args()
 
 
@@ -152,6 +153,25 @@ def distributed():
     return world, rank, local
 
 
+def max_over_ranks(value: float, world: int) -> float:
+    """The largest of every rank's value (the slowest rank's time): one
+    all-reduce on the process group's own backend."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    device = f"cuda:{torch.cuda.current_device()}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def partition(count: int, rank: int, world: int) -> list:
+    """The units (scenes, requests) rank `rank` of `world` replicas runs:
+    round robin, disjoint, covering all of them; no data crosses ranks."""
+    return list(range(rank, count, max(world, 1)))
+
+
 def cpu_port_rate(scene, threads: int, budget_s: float, max_steps: int, warmup: int) -> tuple[float, int, float]:
     """Oracle steps on `threads` host cores until the budget is spent."""
     import oracle
@@ -177,7 +197,7 @@ def run_reference(args):
     from diaphane_gb300 import workloads
     threads = os.cpu_count() or 1
     scene = workloads.heterogeneous(args.side)
-    rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=60.0, max_steps=args.steps,
+    rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=args.ref_budget, max_steps=args.steps,
                                          warmup=min(args.warmup, 1))
     sample = (f"{steps} oracle steps of the full {args.side}^3 scene in {elapsed:.1f} s "
               f"(time-budgeted; the per-step cost is constant)")
@@ -234,12 +254,7 @@ def run_ours(args):
         sim.wait(600_000)
         barrier()
     launches = sim.launch_count() - launches0
-    ms = start.elapsed_time(end)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(start.elapsed_time(end), world)
     seconds = ms / 1e3
     value = world * cells * args.steps / seconds / 1e9
 
@@ -260,12 +275,7 @@ def run_ours(args):
         sim.advance_by(args.steps)
         read_into(sim, pinned_i, pinned_e, pinned_h)
         barrier()
-        e2e_s = time.perf_counter() - t0
-        if world > 1:
-            import torch.distributed as dist
-            t = torch.tensor([e2e_s], device=f"cuda:{device}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(time.perf_counter() - t0, world)
         h2d = 24 * cells / args.steps
         d2h = 28 * cells / args.steps
         e2e = {"value": world * cells * args.steps / e2e_s / 1e9, "unit": "Gcell/s",
@@ -273,6 +283,16 @@ def run_ours(args):
                "what": "restore E,H from pinned host memory; advance K steps with intensity; "
                        "read intensity, E and H back; wall clock"}
 
+    # Every rank takes part in the batch measurement (its scenes, then the
+    # slowest rank's time); the rest is rank 0's.
+    kernel_name = ["", "fused", "naive"][sim.kernel]
+    batched = None
+    if not args.no_batched:
+        sim.close()
+        try:
+            batched = batched_measurement(args.scenes, args.batch_steps, device, rank, world)
+        except Exception as exc:  # reported, not fatal to the headline line
+            batched = {"error": f"{type(exc).__name__}: {exc}"}
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -288,14 +308,6 @@ def run_ours(args):
         rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=12.0, max_steps=200, warmup=0)
         cpu = {"value": rate, "unit": "Gcell/s", "cores": threads, "kind": "port",
                "sample": f"{steps} oracle steps of the same {args.side}^3 scene, {elapsed:.1f} s"}
-    kernel_name = ["", "fused", "naive"][sim.kernel]
-    batched = None
-    if world == 1 and not args.no_batched:
-        sim.close()
-        try:
-            batched = batched_measurement(args.scenes, args.batch_steps, device)
-        except Exception as exc:  # reported, not fatal to the headline line
-            batched = {"error": f"{type(exc).__name__}: {exc}"}
     line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64 scene)",
@@ -325,7 +337,7 @@ def read_into(sim, intensity, electric, magnetic) -> None:
 BATCH_SEED = 0xBA7C_0000
 
 
-def batched_measurement(scene_count: int, steps: int, device: int = 0) -> dict:
+def batched_measurement(scene_count: int, steps: int, device: int = 0, rank: int = 0, world: int = 1) -> dict:
     """Mixed-size batch vs this project's plain one-scene-at-a-time solver.
 
     Scenes: axes log-uniform in [32, 160] cells, seeded spheres, an optional
@@ -334,8 +346,10 @@ def batched_measurement(scene_count: int, steps: int, device: int = 0) -> dict:
     allocation, upload, stepping and reading every scene's E field back."""
     import numpy as np
     from diaphane_gb300 import Batch, ResolvedScene, Simulation, workloads
-    resolved = [ResolvedScene(workloads.mixed_scene(BATCH_SEED + k)) for k in range(scene_count)]
-    cells = sum(r.cells for r in resolved)
+    mine = partition(scene_count, rank, world)  # replicas split the scenes; nothing is exchanged
+    resolved = [ResolvedScene(workloads.mixed_scene(BATCH_SEED + k)) for k in mine]
+    cells = sum(ResolvedScene(workloads.mixed_scene(BATCH_SEED + k)).cells for k in range(scene_count)) \
+        if world > 1 else sum(r.cells for r in resolved)
     # Plain: one Simulation per scene, one after another.
     plain_out = {}
     t0 = time.perf_counter()
@@ -346,22 +360,23 @@ def batched_measurement(scene_count: int, steps: int, device: int = 0) -> dict:
         if k < 4:
             plain_out[k] = e
         sim.close()
-    plain_s = time.perf_counter() - t0
+    plain_s = max_over_ranks(time.perf_counter() - t0, world)
     # Batched: one arena, one launch per step per kernel variant, K-step graphs.
     arena = int(1.05 * sum(Batch.bytes_for(r, steps) for r in resolved)) + (64 << 20)
-    batch = Batch(arena, chunk_steps=50, max_scenes=scene_count, device=device)
+    batch = Batch(arena, chunk_steps=50, max_scenes=max(1, len(resolved)), device=device)
     t0 = time.perf_counter()
     ids = [batch.add(r, steps) for r in resolved]
     batch.run_to_completion()
     outs = [batch.read_electric(i) for i in ids]
-    batched_s = time.perf_counter() - t0
+    batched_s = max_over_ranks(time.perf_counter() - t0, world)
     identical = all(np.array_equal(outs[k].view(np.uint32), plain_out[k].view(np.uint32)) for k in plain_out)
     return {"scenes": scene_count, "steps": steps, "cells": cells,
             "batched_solves_per_s": scene_count / batched_s, "plain_solves_per_s": scene_count / plain_s,
             "speedup": plain_s / batched_s, "batched_gcells": cells * steps / batched_s / 1e9,
             "plain_gcells": cells * steps / plain_s / 1e9, "batched_s": batched_s, "plain_s": plain_s,
             "chunk_steps": 50, "graph_launches": batch.launch_count(),
-            "bit_identical_to_plain": identical}
+            "bit_identical_to_plain": identical, "replicas": world,
+            "scaling": "strong (the 256 scenes are split across replicas)"}
 
 
 def run_batched(args):
