@@ -13,7 +13,8 @@ LIBRARY = Path(__file__).resolve().parent / "libdiaphane_gb300.so"
 DP_OK = 0
 STATUS_NAMES = {0: "DP_OK", 1: "DP_ERR_INVALID", 2: "DP_ERR_LOSSY", 3: "DP_ERR_CUDA", 4: "DP_ERR_TIMEOUT",
                 5: "DP_ERR_OOM", 6: "DP_ERR_UNSUPPORTED", 7: "DP_ERR_RANGE", 8: "DP_ERR_BUSY"}
-DP_ERR_OOM, DP_ERR_BUSY = 5, 8
+DP_ERR_INVALID, DP_ERR_LOSSY, DP_ERR_CUDA, DP_ERR_TIMEOUT = 1, 2, 3, 4
+DP_ERR_OOM, DP_ERR_UNSUPPORTED, DP_ERR_RANGE, DP_ERR_BUSY = 5, 6, 7, 8
 
 DP_BOUNDARY_PEC, DP_BOUNDARY_ABSORBING = 0, 1
 DP_SHAPE_BLOCK, DP_SHAPE_SPHERE, DP_SHAPE_SLAB = 0, 1, 2

@@ -1,0 +1,73 @@
+"""Edge shapes and limits of the GPU path, each against the oracle bit for bit:
+the smallest grids the reference accepts (2 cells on an axis), rows shorter
+than a lane's cells, odd extents, more sources than the fused step carries
+(the handle falls back to the one-thread-per-cell passes), and a zero-step
+advance."""
+import numpy as np
+import pytest
+
+import oracle
+from diaphane_gb300 import (DP_KERNEL_AUTO, DP_KERNEL_FUSED, DP_KERNEL_NAIVE, Axis, Batch, Boundary, DiaphaneError,
+                            Extent, Material, ResolvedScene, Scene, Shape, Source, Waveform)
+from diaphane_gb300 import Simulation
+from diaphane_gb300._abi import DP_ERR_UNSUPPORTED
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return a.view(np.uint32)
+
+
+def small_scene(extent, sources=1):
+    scene = Scene.empty(Extent(*extent), 1e-3).with_boundary(Boundary.PEC)
+    glass = scene.materials.push(Material.dielectric(2.5))
+    scene.shapes.append(Shape.block((0.0, 0.0, 0.0), (2e-3, 2e-3, 2e-3), glass))
+    frequency = scene.grid.frequency_for_resolution(8.0)
+    for k in range(sources):
+        at = [((k * 7 + 3 * a) % max(n, 1) - n / 2 + 0.5) * 1e-3 for a, n in enumerate(extent)]
+        scene.sources.append(Source.point(at, Axis(k % 3), Waveform.ricker(frequency)))
+    return scene
+
+
+@pytest.mark.parametrize("extent", [(2, 2, 2), (3, 5, 7), (4, 2, 9), (5, 3, 2), (130, 3, 2), (33, 2, 40)])
+@pytest.mark.parametrize("kernel", [DP_KERNEL_FUSED, DP_KERNEL_NAIVE])
+def test_small_and_odd_grids_match_the_oracle(extent, kernel, threads):
+    scene = small_scene(extent)
+    ref = oracle.OracleSimulation(scene, threads=threads)
+    sim = Simulation(scene, kernel=kernel)
+    assert sim.kernel == kernel
+    ref.advance_by(40)
+    sim.advance_by(40)
+    assert np.array_equal(bits(sim.read_electric()), bits(ref.read_electric())), extent
+    assert np.array_equal(bits(sim.read_magnetic()), bits(ref.read_magnetic())), extent
+
+
+def test_more_sources_than_the_fused_step_carries_fall_back_exactly(threads):
+    scene = small_scene((24, 20, 18), sources=17)
+    with pytest.raises(DiaphaneError) as err:
+        Simulation(scene, kernel=DP_KERNEL_FUSED)
+    assert err.value.status == DP_ERR_UNSUPPORTED
+    sim = Simulation(scene, kernel=DP_KERNEL_AUTO)
+    assert sim.kernel == DP_KERNEL_NAIVE
+    ref = oracle.OracleSimulation(scene, threads=threads)
+    sim.advance_by(60)
+    ref.advance_by(60)
+    assert np.array_equal(bits(sim.read_electric()), bits(ref.read_electric()))
+    assert np.array_equal(bits(sim.read_magnetic()), bits(ref.read_magnetic()))
+
+
+def test_a_zero_step_advance_changes_nothing():
+    sim = Simulation(small_scene((16, 12, 10)))
+    sim.advance_by(7)
+    before = sim.read_electric()
+    sim.advance_by(0)
+    assert sim.step_count() == 7
+    assert np.array_equal(bits(sim.read_electric()), bits(before))
+
+
+def test_a_batch_refuses_a_scene_with_too_many_sources():
+    batch = Batch(1 << 28, chunk_steps=4, max_scenes=2)
+    with pytest.raises(DiaphaneError) as err:
+        batch.add(ResolvedScene(small_scene((16, 12, 10), sources=5)), 10)
+    assert err.value.status == DP_ERR_UNSUPPORTED
