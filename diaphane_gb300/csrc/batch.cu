@@ -280,6 +280,10 @@ struct dp_batch {
 
     // One chunk: stage descriptors and injections, then replay (or launch).
     uint32_t run_chunk() {
+        // A chunk right after a membership change launches directly: a graph
+        // pays off only once it is replayed, and membership that changes
+        // every chunk (requests arriving and leaving) would never replay one.
+        const bool changed = dirty;
         if (dirty) rebuild_lists();
         const int half = stage;
         // The staging half is free once the copies that last read it are done.
@@ -331,7 +335,7 @@ struct dp_batch {
               "counts");
         check(cudaEventRecord(staged[half], stream), "staging event");
         if (stepping) {
-            if (graphs) {
+            if (graphs && !changed) {
                 if (!exec[half]) {
                     cudaGraph_t graph = nullptr;
                     check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "capture");

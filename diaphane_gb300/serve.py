@@ -101,15 +101,16 @@ class Server:
             active[ident] = r
             queue.popleft()
 
-    def _retire(self, active: dict, t0: float) -> None:
-        for ident in list(active):
-            step, target = self.batch.status(ident)
-            if step >= target:
-                r = active.pop(ident)
-                r.series = self.batch.read_probes(ident)
-                self.batch.remove(ident)
-                r.done = self.clock() - t0
-                r.resolved = None  # the host copy of the scene is no longer needed
+    def _finished(self, active: dict) -> list:
+        return [ident for ident in active if self.batch.status(ident)[0] >= self.batch.status(ident)[1]]
+
+    def _retire(self, active: dict, finished: list, t0: float) -> None:
+        for ident in finished:
+            r = active.pop(ident)
+            r.series = self.batch.read_probes(ident)  # waits for the chunk that finished it
+            self.batch.remove(ident)
+            r.done = self.clock() - t0
+            r.resolved = None  # the host copy of the scene is no longer needed
 
     def serve(self, trace: list[Request]) -> list[Request]:
         pending = deque(sorted(trace, key=lambda r: r.arrival))
@@ -124,15 +125,18 @@ class Server:
             self.peak_active = max(self.peak_active, len(active))
             if active:
                 c0 = self.clock()
-                self.batch.advance_chunk()
+                self.batch.advance_chunk()  # queued; at most two chunks run ahead of the host
                 self.chunks += 1
                 # Host scene setup of the next arrivals overlaps the chunk.
                 for r in list(pending)[:4]:
                     if r.arrival <= self.clock() - t0 + 0.05:
                         r.resolve()
-                self.batch.wait()
+                # Wait only when a request's last step was just issued.
+                finished = self._finished(active)
+                if finished:
+                    self.batch.wait()
+                    self._retire(active, finished, t0)
                 self.busy_seconds += self.clock() - c0
-                self._retire(active, t0)
             elif pending:
                 pending[0].resolve()
                 delay = pending[0].arrival - (self.clock() - t0)
