@@ -29,6 +29,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import platform
 import statistics
 import subprocess
 import sys
@@ -191,6 +192,24 @@ def cpu_port_rate(scene, threads: int, budget_s: float, max_steps: int, warmup: 
     return cells * steps / elapsed / 1e9, steps, elapsed
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            if line.lower().startswith(("model name", "cpu model")):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return platform.processor() or platform.machine()
+
+
 def run_reference(args):
     world, rank, _ = distributed()
     if rank != 0:
@@ -206,7 +225,8 @@ def run_reference(args):
             "steps": steps, "warmup": min(args.warmup, 1), "ms_per_step": 1e3 * elapsed / max(steps, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded SplitMix64 scene)", "config": config(args.side, world),
-            "cpu_baseline": {"value": rate, "unit": "Gcell/s", "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": rate, "unit": "Gcell/s", "cores": threads, "kind": "port", "sample": sample,
+                             "nproc": os.cpu_count(), "cpu_model": cpu_model()},
             "e2e": {"value": rate, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference is Rust (cargo absent on both machines); this is the oracle's C++ restatement "
                     "of src/cpu.rs with OpenMP over z planes"}
@@ -307,8 +327,12 @@ def run_ours(args):
     if world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=12.0, max_steps=200, warmup=0)
+        rate1, steps1, elapsed1 = cpu_port_rate(scene, 1, budget_s=8.0, max_steps=50, warmup=0)
         cpu = {"value": rate, "unit": "Gcell/s", "cores": threads, "kind": "port",
-               "sample": f"{steps} oracle steps of the same {args.side}^3 scene, {elapsed:.1f} s"}
+               "sample": f"{steps} oracle steps of the same {args.side}^3 scene, {elapsed:.1f} s",
+               "single_thread": {"value": rate1, "unit": "Gcell/s", "cores": 1,
+                                 "sample": f"{steps1} oracle steps, {elapsed1:.1f} s"},
+               "nproc": os.cpu_count(), "cpu_model": cpu_model()}
     line = {"metric": "Gcell-updates/s", "value": value, "unit": "Gcell/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64 scene)",
