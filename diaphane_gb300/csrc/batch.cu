@@ -158,6 +158,7 @@ struct dp_batch {
     uint32_t chunk = 50;
     uint32_t capacity = 0;        // scene slots
     uint32_t cells_per_lane = 0;  // forced tile width (0: per scene)
+    uint32_t unit_planes = 24;    // z-planes per work unit
     bool graphs = true;
     unsigned char *arena_base = nullptr;
     Arena arena;
@@ -410,14 +411,13 @@ Layout layout_of(const Scene &s, uint32_t probe_count, uint64_t steps) {
     return l;
 }
 
-void make_units(Entry &e, int sm_count) {
+void make_units(Entry &e, uint32_t planes) {
     const uint32_t *n = e.scene.grid.n;
     const uint32_t tx = 32 * e.variant.cx, ty = e.variant.tile_y;
     const uint32_t tiles_x = (n[0] + tx - 1) / tx, tiles_y = (n[1] + ty - 1) / ty;
-    // Units of about 24 planes: enough planes to amortize a unit's start-up
-    // (one extra H plane, ring fill), small enough to spread a scene.
-    (void)sm_count;
-    const uint32_t depth = std::max<uint32_t>(8, std::min<uint32_t>(24, n[2]));
+    // Units of `planes` planes (at least 8): enough to amortize a unit's
+    // start-up (one extra H plane, ring fill), few enough to spread a scene.
+    const uint32_t depth = std::max<uint32_t>(8, std::min<uint32_t>(planes, n[2]));
     e.units.clear();
     for (uint32_t z0 = 0; z0 < n[2]; z0 += depth)
         for (uint32_t ty_i = 0; ty_i < tiles_y; ++ty_i)
@@ -442,6 +442,7 @@ dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out) {
             opts->cells_per_lane != 4)
             throw Error(DP_ERR_INVALID, "cells_per_lane must be 0, 1, 2 or 4");
         b->cells_per_lane = opts->cells_per_lane;
+        b->unit_planes = opts->unit_planes ? opts->unit_planes : 24;
         if (opts->arena_bytes == 0) throw Error(DP_ERR_INVALID, "arena_bytes must be positive");
         b->bind();
         check(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "stream");
@@ -558,9 +559,7 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
             }
             e.probe_cells.push_back(uint32_t((uint64_t(c[2]) * s.grid.n[1] + c[1]) * l.pitch + c[0]));
         }
-        int sms = 0;
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device);
-        make_units(e, sms);
+        make_units(e, b->unit_planes);
         b->slot_used[slot] = 1;
         *id = e.id;
         b->entries.emplace(e.id, std::move(e));
