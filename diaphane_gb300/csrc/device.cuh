@@ -107,7 +107,6 @@ struct FusedMaps {
     alignas(64) unsigned char h[128];
     alignas(64) unsigned char m[128];
 };
-bool fused_supported(const uint32_t n[3]);
 bool fused_variant_exists(uint32_t cx, uint32_t tile_y, uint32_t slots);
 // Zero for cx, tile_y, slots or z_chunk picks the default.
 FusedPlan fused_plan(const uint32_t n[3], uint32_t cx, uint32_t tile_y, uint32_t slots, uint32_t z_chunk,

@@ -51,7 +51,6 @@ constexpr long long kWaitCycles = 1ll << 32; // ~2 s at 2 GHz, then give up
 // CX cells per lane along x, TY rows per tile (one warp each), SLOTS planes
 // in the shared-memory ring.
 template <int CX, int TY, int SLOTS> struct Geometry {
-    static constexpr int kTileY = TY;
     static constexpr int kWarps = TY;
     static constexpr int kThreads = 32 * TY;
     static constexpr int kSlots = SLOTS;
@@ -210,10 +209,6 @@ __device__ __forceinline__ float h_full(float h, float loss, float gain, float c
     return exact_div((1.0f - loss) * h - gain * curl, 1.0f + loss);
 }
 
-__device__ __forceinline__ float e_full(float e, float loss, float gain, float curl) {
-    return exact_div((1.0f - loss) * e + gain * curl, 1.0f + loss);
-}
-
 // Bit k is set when injection k of `magnetic` phase covers row y and any of
 // the cells [xa, xb).  Computed once per thread; the per-plane test is then a
 // single z comparison per set bit.
@@ -313,7 +308,7 @@ template <int CX, int TY, int SLOTS>
 __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUtensorMap *h_map_p,
                                           const CUtensorMap *m_map_p, const UnitArgs &u) {
     using G = Geometry<CX, TY, SLOTS>;
-    constexpr int kTileY = G::kTileY, kWarps = G::kWarps, kThreads = G::kThreads, kSlots = G::kSlots;
+    constexpr int kWarps = G::kWarps, kThreads = G::kThreads, kSlots = G::kSlots;
     extern __shared__ __align__(128) unsigned char smem[];
     const DeviceScene &s = u.s;
     const InjectionView &inj = u.inj;
@@ -743,7 +738,8 @@ EncodeTiled encoder() {
     static EncodeTiled fn = [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q{};
-        if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) != cudaSuccess ||
+        // The entry point as introduced in CUDA 12.0.
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
             q != cudaDriverEntryPointSuccess || p == nullptr)
             return EncodeTiled(nullptr);
         return reinterpret_cast<EncodeTiled>(p);
@@ -770,13 +766,6 @@ template <int CX, int TY, int SLOTS> void configure() {
     cudaFuncSetAttribute(fused_step<CX, TY, SLOTS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     done = true;
 }
-
-// The kernel variants this library carries: (cells per lane, rows per tile,
-// ring depth).  Each fits 16 resident warps per SM at 128 registers.
-struct Variant {
-    uint32_t cx, ty, slots;
-};
-constexpr Variant kVariants[] = {{4, 8, 3}, {2, 8, 5}, {4, 16, 3}, {1, 8, 5}};
 
 template <int CX, int TY, int SLOTS> size_t smem_of() { return Geometry<CX, TY, SLOTS>::SMEM; }
 
@@ -811,11 +800,6 @@ void launch_variant(const FusedPlan &plan, const FusedMaps &m, const FusedArgs &
 }
 
 } // namespace
-
-bool fused_supported(const uint32_t n[3]) {
-    // TMA needs 16-byte row strides for the f32 fields.
-    return n[0] % 4 == 0 && n[0] >= 4 && n[1] >= 2 && n[2] >= 2 && encoder() != nullptr;
-}
 
 bool fused_variant_exists(uint32_t cx, uint32_t ty, uint32_t slots) { return variant_smem(cx, ty, slots) != 0; }
 
