@@ -78,7 +78,8 @@ class dp_grid_info(C.Structure):
 
 class dp_scene_info(C.Structure):
     _fields_ = [("extent", U3), ("material_count", C.c_uint32), ("time_step", C.c_float),
-                ("courant", C.c_float), ("absorber_peak", C.c_float), ("reversible", C.c_int32)]
+                ("courant", C.c_float), ("absorber_peak", C.c_float), ("reversible", C.c_int32),
+                ("index_bytes", C.c_uint32)]
 
 
 class dp_injection(C.Structure):

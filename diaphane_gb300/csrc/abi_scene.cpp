@@ -112,6 +112,7 @@ dp_status dp_scene_info_get(const dp_scene *scene, dp_scene_info *out) {
         out->courant = s.grid.courant;
         out->absorber_peak = s.absorber_peak;
         out->reversible = s.reversible ? 1 : 0;
+        out->index_bytes = s.index_bytes;
         return DP_OK;
     });
 }

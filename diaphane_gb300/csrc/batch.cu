@@ -480,6 +480,7 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         if (!tensor_maps_available()) throw Error(DP_ERR_UNSUPPORTED, "the driver offers no tensor-map encoder");
         if (2 * s.sources.size() > size_t(kBatchInjections))
             throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 4 sources");
+        if (s.index_bytes != 1) throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 256 materials");
         uint32_t slot = 0;
         while (slot < b->capacity && b->slot_used[slot]) ++slot;
         if (slot == b->capacity) throw Error(DP_ERR_BUSY, "every scene slot of the batch is in use");

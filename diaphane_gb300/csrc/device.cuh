@@ -17,13 +17,19 @@ struct DeviceScene {
     uint32_t n[3];
     uint32_t pitch;          // row stride in cells (nx, or nx rounded up to 4 in a batch arena)
     uint64_t cells;          // component stride: pitch * ny * nz
-    const uint8_t *material; // cells
+    const uint8_t *material; // cells, u8 index (scenes of up to 256 materials)
+    const uint16_t *material16; // cells, u16 index (wider scenes; material is null then)
     const float4 *coeff;     // (electric_gain, electric_loss, magnetic_gain, magnetic_loss)
     const float *mgain;      // nx | ny | nz, c*dt/primary width
     const float *egain;      // nx | ny | nz, c*dt/dual width
     const float *absorber;   // integer x|y|z, then half x|y|z
     const float *weights;    // sheet apodization planes
 };
+
+// The material of cell i, whichever width the index has.
+__device__ __forceinline__ uint32_t material_of(const DeviceScene &s, uint64_t i) {
+    return s.material16 ? uint32_t(s.material16[i]) : uint32_t(s.material[i]);
+}
 
 // One injection of one step (Injection, src/source.rs:409-427).
 struct DeviceInjection {
@@ -79,7 +85,7 @@ void copy_fields_in(float *device, const float *host, const uint32_t n[3], uint3
 // Scene::material_indices on the device (raster.cu): the u8 index with rows of
 // `pitch` bytes (padding cells 0), asynchronous on `stream`.
 struct Scene;
-void rasterize_on_device(const Scene &s, uint8_t *out, uint32_t pitch, cudaStream_t stream);
+void rasterize_on_device(const Scene &s, void *out, uint32_t pitch, cudaStream_t stream);
 
 // Reductions (kernels_naive.cu).
 void launch_energy(const DeviceScene &s, FieldSet f, const float *primary, const float *dual,

@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(kThreads) magnetic_pass(DeviceScene s, const T
     const uint64_t stride[3] = {1, s.pitch, uint64_t(s.pitch) * s.n[1]};
     const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
     const uint32_t span = s.n[0] + s.n[1] + s.n[2];
-    const float4 k = s.coeff[s.material[i]];
+    const float4 k = s.coeff[material_of(s, i)];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const int b = (a + 1) % 3, cc = (a + 2) % 3;
@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(kThreads) electric_pass(DeviceScene s, const T
     const uint64_t stride[3] = {1, s.pitch, uint64_t(s.pitch) * s.n[1]};
     const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
     const uint32_t span = s.n[0] + s.n[1] + s.n[2];
-    const float4 k = s.coeff[s.material[i]];
+    const float4 k = s.coeff[material_of(s, i)];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
         const int b = (a + 1) % 3, cc = (a + 2) % 3;
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(kThreads) energy_pass(DeviceScene s, Fields<T>
          i += uint64_t(gridDim.x) * kThreads) {
         uint32_t c[3];
         if (!decompose(i, s, c)) continue;
-        const float2 m = eps_mu[s.material[i]];
+        const float2 m = eps_mu[material_of(s, i)];
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
             const int b = (a + 1) % 3, cc = (a + 2) % 3;

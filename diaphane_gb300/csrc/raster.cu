@@ -1,5 +1,6 @@
-// Device rasterization of a scene's shapes into the u8 material index
-// (Scene::material_indices, src/scene.rs:181-206): a cell takes the material
+// Device rasterization of a scene's shapes into the material index (u8, or
+// u16 past 256 materials; Scene::material_indices, src/scene.rs:181-206):
+// a cell takes the material
 // of the last shape, in scene order, that contains its centre
 // (Shape::contains, src/scene.rs:60-81).
 //
@@ -46,9 +47,10 @@ __device__ __forceinline__ bool contains(const dp_shape &s, const float p[3]) {
     return fabsf(p[s.axis] - s.offset) <= 0.5f * s.thickness;
 }
 
+template <typename T>
 __global__ void __launch_bounds__(kRasterThreads)
 raster_pass(const float *__restrict__ centers, uint32_t nx, uint32_t ny, uint32_t pitch,
-            const RasterShape *__restrict__ shapes, uint32_t count, uint8_t *__restrict__ out) {
+            const RasterShape *__restrict__ shapes, uint32_t count, T *__restrict__ out) {
     __shared__ uint32_t list[kRasterThreads];
     __shared__ uint32_t warp_hits[kRasterWarps];
     const uint32_t segments = (pitch + kRasterThreads - 1) / kRasterThreads;
@@ -88,17 +90,18 @@ raster_pass(const float *__restrict__ centers, uint32_t nx, uint32_t ny, uint32_
             }
         __syncthreads(); // the list is rewritten by the next batch
     }
-    if (x < pitch) out[row * pitch + x] = x < nx ? uint8_t(material) : uint8_t(0);
+    if (x < pitch) out[row * pitch + x] = x < nx ? T(material) : T(0);
 }
 
 } // namespace
 
 namespace diaphane {
 
-// Rasterizes into `out` (device, rows of `pitch` >= nx bytes, padding cells
-// set to 0), asynchronously on `stream`.  The shape table and the cell
-// centres go up through stream-ordered allocations freed on the same stream.
-void rasterize_on_device(const Scene &s, uint8_t *out, uint32_t pitch, cudaStream_t stream) {
+// Rasterizes into `out` (device, index_bytes per cell, rows of `pitch` >= nx
+// cells, padding cells set to 0), asynchronously on `stream`.  The shape
+// table and the cell centres go up through stream-ordered allocations freed
+// on the same stream.
+void rasterize_on_device(const Scene &s, void *out, uint32_t pitch, cudaStream_t stream) {
     const uint32_t *n = s.grid.n;
     if (pitch < n[0]) throw Error(DP_ERR_INVALID, "row pitch narrower than the grid");
     std::vector<RasterShape> table;
@@ -135,8 +138,12 @@ void rasterize_on_device(const Scene &s, uint8_t *out, uint32_t pitch, cudaStrea
     const uint64_t segments = (pitch + kRasterThreads - 1) / kRasterThreads;
     const uint64_t blocks = segments * n[1] * n[2];
     if (blocks > 0x7fffffffull) throw Error(DP_ERR_RANGE, "grid too large for the rasterizer's launch");
-    raster_pass<<<unsigned(blocks), kRasterThreads, 0, stream>>>(d_centers, n[0], n[1], pitch, d_shapes,
-                                                                uint32_t(table.size()), out);
+    if (s.index_bytes == 1)
+        raster_pass<uint8_t><<<unsigned(blocks), kRasterThreads, 0, stream>>>(
+            d_centers, n[0], n[1], pitch, d_shapes, uint32_t(table.size()), static_cast<uint8_t *>(out));
+    else
+        raster_pass<uint16_t><<<unsigned(blocks), kRasterThreads, 0, stream>>>(
+            d_centers, n[0], n[1], pitch, d_shapes, uint32_t(table.size()), static_cast<uint16_t *>(out));
     check(cudaGetLastError(), "raster launch");
     check(cudaFreeAsync(d_shapes, stream), "raster free");
     check(cudaFreeAsync(d_centers, stream), "raster free");
@@ -144,7 +151,7 @@ void rasterize_on_device(const Scene &s, uint8_t *out, uint32_t pitch, cudaStrea
 
 } // namespace diaphane
 
-extern "C" dp_status dp_scene_raster(const dp_scene *scene, uint8_t *device_out, uint32_t row_pitch, void *stream) {
+extern "C" dp_status dp_scene_raster(const dp_scene *scene, void *device_out, uint32_t row_pitch, void *stream) {
     return guarded([&] {
         if (!scene || !device_out) throw Error(DP_ERR_INVALID, "null argument");
         cudaStream_t st = static_cast<cudaStream_t>(stream);

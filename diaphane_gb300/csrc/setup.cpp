@@ -343,7 +343,7 @@ void shape_cell_range(const ResolvedGrid &g, const dp_shape &s, int axis, uint32
 const std::vector<uint8_t> &Scene::material_index() const {
     if (indexed_) return index_cache_;
     const ResolvedGrid &g = grid;
-    index_cache_.assign(g.cells(), 0);
+    index_cache_.assign(g.cells() * index_bytes, 0);
     for (const dp_shape &sh : shapes) {
         uint32_t lo[3], hi[3];
         bool empty = false;
@@ -352,7 +352,7 @@ const std::vector<uint8_t> &Scene::material_index() const {
             if (lo[a] > hi[a]) empty = true;
         }
         if (empty) continue;
-        const uint8_t material = uint8_t(sh.material);
+        const uint32_t material = sh.material;
         const long z0 = lo[2], z1 = hi[2];
 #pragma omp parallel for schedule(dynamic, 1)
         for (long z = z0; z <= z1; ++z) {
@@ -360,10 +360,13 @@ const std::vector<uint8_t> &Scene::material_index() const {
             p[2] = centers[axis_offset(2) + uint32_t(z)];
             for (uint32_t y = lo[1]; y <= hi[1]; ++y) {
                 p[1] = centers[axis_offset(1) + y];
-                uint8_t *row = &index_cache_[(uint64_t(z) * g.n[1] + y) * g.n[0]];
+                const uint64_t row = (uint64_t(z) * g.n[1] + y) * g.n[0];
                 for (uint32_t x = lo[0]; x <= hi[0]; ++x) {
                     p[0] = centers[x];
-                    if (shape_contains(sh, p)) row[x] = material;
+                    if (!shape_contains(sh, p)) continue;
+                    uint8_t *cell = &index_cache_[(row + x) * index_bytes];
+                    cell[0] = uint8_t(material);
+                    if (index_bytes == 2) cell[1] = uint8_t(material >> 8);
                 }
             }
         }
@@ -378,9 +381,11 @@ Scene Scene::build(const dp_scene_desc &d) {
     s.grid.validate();
     s.boundary = d.boundary;
     if (d.material_count == 0 || d.materials == nullptr) invalid("a material table needs vacuum at index 0");
-    if (d.material_count > 256) throw Error(DP_ERR_UNSUPPORTED, "at most 256 materials: the material index is stored as u8");
+    if (d.material_count > 65536)
+        throw Error(DP_ERR_UNSUPPORTED, "at most 65536 materials: the material index is stored as u16");
     if ((d.shape_count && !d.shapes) || (d.source_count && !d.sources)) invalid("null shape or source array");
     s.materials.assign(d.materials, d.materials + d.material_count);
+    s.index_bytes = d.material_count <= 256 ? 1 : 2;
     s.shapes.assign(d.shapes, d.shapes + d.shape_count);
     s.sources.assign(d.sources, d.sources + d.source_count);
     for (const auto &sh : s.shapes)

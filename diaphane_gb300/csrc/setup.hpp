@@ -116,9 +116,11 @@ struct Scene {
     static Scene build(const dp_scene_desc &desc);
 
     // Scene::material_indices (src/scene.rs:181-206) on the host, computed on
-    // first use.  The simulation paths rasterize on the device instead
-    // (raster.cu); this copy serves the table export and host-side checks.
+    // first use: index_bytes bytes per cell (u8 up to 256 materials, else a
+    // little-endian u16).  The simulation paths rasterize on the device
+    // instead (raster.cu); this copy serves the table export and checks.
     const std::vector<uint8_t> &material_index() const;
+    uint32_t index_bytes = 1;
     uint32_t axis_offset(int axis) const { return axis == 0 ? 0 : (axis == 1 ? grid.n[0] : grid.n[0] + grid.n[1]); }
 
     // Source::injections for every source at `time`, two slots per source.

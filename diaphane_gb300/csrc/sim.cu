@@ -80,9 +80,12 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
 
     uint32_t requested = opts ? opts->kernel : DP_KERNEL_AUTO;
     if (requested > DP_KERNEL_NAIVE) throw Error(DP_ERR_INVALID, "unknown kernel selector");
-    const bool fits = tensor_maps_available() && 2 * s.sources.size() <= size_t(kMaxInjections);
+    // The fused step stages the coefficient table in shared memory and reads
+    // a u8 index through its tensor map: at most 256 materials.
+    const bool fits = tensor_maps_available() && 2 * s.sources.size() <= size_t(kMaxInjections) && s.index_bytes == 1;
     if (requested == DP_KERNEL_FUSED && !fits)
-        throw Error(DP_ERR_UNSUPPORTED, "the fused step does not cover this grid shape or source count");
+        throw Error(DP_ERR_UNSUPPORTED,
+                    "the fused step takes at most 16 sources and 256 materials (and needs the tensor-map encoder)");
     sim->kernel = (requested == DP_KERNEL_NAIVE || !fits) ? DP_KERNEL_NAIVE : DP_KERNEL_FUSED;
 
     DeviceScene &d = sim->dev;
@@ -91,12 +94,13 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
     d.cells = cells;
     {
         // The index is rasterized on the device, straight into its buffer.
-        uint8_t *material = device_alloc<uint8_t>(cells, owned);
+        uint8_t *material = device_alloc<uint8_t>(cells * s.index_bytes, owned);
         rasterize_on_device(s, material, sim->pitch, st);
-        d.material = material;
+        d.material = s.index_bytes == 1 ? material : nullptr;
+        d.material16 = s.index_bytes == 2 ? reinterpret_cast<const uint16_t *>(material) : nullptr;
     }
     // Padded to all 256 u8 indices, so a kernel may stage the whole table.
-    std::vector<float4> coeff(256, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+    std::vector<float4> coeff(std::max<size_t>(256, s.coefficients.size()), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
     for (size_t m = 0; m < s.coefficients.size(); ++m) {
         const Coeff &c = s.coefficients[m];
         coeff[m] = make_float4(c.electric_gain, c.electric_loss, c.magnetic_gain, c.magnetic_loss);

@@ -137,10 +137,11 @@ dp_status dp_sim64_create(const dp_scene *scene, int32_t device, dp_sim64 **out)
         for (int a = 0; a < 3; ++a) d.n[a] = s.grid.n[a];
         d.pitch = s.grid.n[0]; // dense rows: the one-thread-per-cell passes need no padding
         d.cells = cells;
-        uint8_t *material = sim->alloc<uint8_t>(cells);
+        uint8_t *material = sim->alloc<uint8_t>(cells * s.index_bytes);
         rasterize_on_device(s, material, s.grid.n[0], sim->stream);
-        d.material = material;
-        std::vector<float4> coeff(256, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+        d.material = s.index_bytes == 1 ? material : nullptr;
+        d.material16 = s.index_bytes == 2 ? reinterpret_cast<const uint16_t *>(material) : nullptr;
+        std::vector<float4> coeff(std::max<size_t>(256, s.coefficients.size()), make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         for (size_t m = 0; m < s.coefficients.size(); ++m) {
             const Coeff &c = s.coefficients[m];
             coeff[m] = make_float4(c.electric_gain, c.electric_loss, c.magnetic_gain, c.magnetic_loss);

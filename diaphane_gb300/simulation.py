@@ -58,6 +58,7 @@ class ResolvedScene:
         self.absorber_peak = info.absorber_peak
         self.reversible = bool(info.reversible)
         self.material_count = info.material_count
+        self.index_bytes = info.index_bytes
 
     def __del__(self):
         if getattr(self, "handle", None):
@@ -66,7 +67,8 @@ class ResolvedScene:
 
     def rasterize(self, device_ptr: int, row_pitch: int = 0, stream: int = 0) -> None:
         """The material index rasterized on the GPU into device memory at
-        `device_ptr` (rows of `row_pitch` bytes, 0 = nx), on `stream`."""
+        `device_ptr` (index_bytes per cell, rows of `row_pitch` cells, 0 = nx),
+        on `stream`."""
         _abi.check(_abi.lib().dp_scene_raster(self.handle, C.c_void_p(device_ptr), row_pitch, C.c_void_p(stream)))
 
     def table(self, which: int) -> np.ndarray:
@@ -77,7 +79,7 @@ class ResolvedScene:
             _abi.DP_TABLE_CELL_CENTERS: (span, np.float32),
             _abi.DP_TABLE_ABSORBER: (2 * span, np.float32),
             _abi.DP_TABLE_COEFFICIENTS: (4 * self.material_count, np.float32),
-            _abi.DP_TABLE_MATERIAL_INDEX: (self.cells, np.uint8),
+            _abi.DP_TABLE_MATERIAL_INDEX: (self.cells, np.uint8 if self.index_bytes == 1 else np.uint16),
             _abi.DP_TABLE_PRIMARY: (span, np.float32),
             _abi.DP_TABLE_DUAL: (span, np.float32),
         }

@@ -183,6 +183,7 @@ typedef struct dp_scene_info {
     float courant;
     float absorber_peak;   /* AbsorbingProfile::peak, src/boundary.rs:215-221 */
     int32_t reversible;    /* Simulation::is_reversible, src/cpu.rs:209-215 */
+    uint32_t index_bytes;  /* bytes per cell of the material index: 1 up to 256 materials, else 2 */
 } dp_scene_info;
 
 /* Tables a kernel consumes, readable for parity checks. */
@@ -217,12 +218,13 @@ void dp_scene_destroy(dp_scene *scene);
 dp_status dp_scene_info_get(const dp_scene *scene, dp_scene_info *out);
 /* Copies one table; bytes must equal the table's size exactly. */
 dp_status dp_scene_table(const dp_scene *scene, uint32_t table, void *host, size_t bytes);
-/* Scene::material_indices (src/scene.rs:181-206) on the GPU: writes the u8
- * index into caller-owned device memory with rows of `row_pitch` bytes
- * (0 = nx; padding bytes are set to 0), asynchronously on `stream` (a
- * cudaStream_t, or null for the default stream).  Identical to the
- * DP_TABLE_MATERIAL_INDEX table, which is rasterized on the host. */
-dp_status dp_scene_raster(const dp_scene *scene, uint8_t *device_out, uint32_t row_pitch, void *stream);
+/* Scene::material_indices (src/scene.rs:181-206) on the GPU: writes the
+ * index (index_bytes per cell: u8, or u16 past 256 materials) into
+ * caller-owned device memory with rows of `row_pitch` cells (0 = nx; padding
+ * cells are set to 0), asynchronously on `stream` (a cudaStream_t, or null
+ * for the default stream).  Identical to the DP_TABLE_MATERIAL_INDEX table,
+ * which is rasterized on the host. */
+dp_status dp_scene_raster(const dp_scene *scene, void *device_out, uint32_t row_pitch, void *stream);
 /* Source::injections (src/source.rs:280-403) for every source at `time`,
  * silenced slots included: 2 per source, in source order. */
 dp_status dp_scene_injections(const dp_scene *scene, float time, dp_injection *out,

@@ -71,3 +71,30 @@ def test_a_batch_refuses_a_scene_with_too_many_sources():
     with pytest.raises(DiaphaneError) as err:
         batch.add(ResolvedScene(small_scene((16, 12, 10), sources=5)), 10)
     assert err.value.status == DP_ERR_UNSUPPORTED
+
+
+def test_past_256_materials_the_index_widens_and_stays_exact(threads):
+    """The reference indexes materials with u32; past 256 this library keeps a
+    u16 index, steps with the one-thread-per-cell passes (the fused step and
+    the batch stage a u8 index) and matches the oracle bit for bit."""
+    from tests.test_setup_parity import many_materials
+    scene = many_materials(300, side=28)
+    frequency = scene.grid.frequency_for_resolution(8.0)
+    scene.sources.append(Source.point((0.0005, 0.0, 0.0), Axis.Z, Waveform.ricker(frequency)))
+    resolved = ResolvedScene(scene)
+    assert resolved.index_bytes == 2
+    with pytest.raises(DiaphaneError) as err:
+        Simulation(resolved, kernel=DP_KERNEL_FUSED)
+    assert err.value.status == DP_ERR_UNSUPPORTED
+    with pytest.raises(DiaphaneError) as err:
+        Batch(1 << 28, chunk_steps=4, max_scenes=2).add(resolved, 10)
+    assert err.value.status == DP_ERR_UNSUPPORTED
+    sim = Simulation(resolved)
+    assert sim.kernel == DP_KERNEL_NAIVE
+    ref = oracle.OracleSimulation(scene, threads=threads)
+    sim.advance_by(60)
+    ref.advance_by(60)
+    assert np.array_equal(bits(sim.read_electric()), bits(ref.read_electric()))
+    assert np.array_equal(bits(sim.read_magnetic()), bits(ref.read_magnetic()))
+    e, m = sim.energy(), ref.energy()
+    assert e.total() == pytest.approx(m.total(), rel=1e-9)

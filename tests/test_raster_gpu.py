@@ -14,10 +14,14 @@ pytestmark = pytest.mark.gpu
 
 def device_index(resolved, pitch):
     nx, ny, nz = resolved.extent
-    buf = torch.full((nz * ny * pitch,), 0xAB, dtype=torch.uint8, device="cuda")
+    dtype = torch.uint8 if resolved.index_bytes == 1 else torch.int16
+    buf = torch.full((nz * ny * pitch,), 0x2B, dtype=dtype, device="cuda")
     resolved.rasterize(buf.data_ptr(), pitch)
     torch.cuda.synchronize()
-    return buf.cpu().numpy().reshape(nz * ny, pitch)
+    out = buf.cpu().numpy()
+    if resolved.index_bytes == 2:
+        out = out.view(np.uint16)
+    return out.reshape(nz * ny, pitch)
 
 
 def blocks_and_slabs():
@@ -39,6 +43,7 @@ CASES = {
     "materials": lambda: scenes.materials()[0],
     "mixed 1": lambda: workloads.mixed_scene(11, lo=33, hi=70),
     "mixed 2": lambda: workloads.mixed_scene(12, lo=33, hi=70),
+    "300 materials (u16 index)": lambda: __import__("tests.test_setup_parity", fromlist=["x"]).many_materials(300, 26),
 }
 
 
@@ -47,7 +52,8 @@ def test_device_raster_matches_the_oracle(case):
     scene = CASES[case]()
     resolved = ResolvedScene(scene)
     nx, ny, nz = resolved.extent
-    expected = oracle.OracleSimulation(scene).table(_abi.DP_TABLE_MATERIAL_INDEX).astype(np.uint8)
+    dtype = np.uint8 if resolved.index_bytes == 1 else np.uint16
+    expected = oracle.OracleSimulation(scene).table(_abi.DP_TABLE_MATERIAL_INDEX).astype(dtype)
     assert np.array_equal(resolved.table(_abi.DP_TABLE_MATERIAL_INDEX), expected)
     for pitch in (nx, (nx + 3) // 4 * 4, (nx + 15) // 16 * 16 + 16):
         rows = device_index(resolved, pitch)

@@ -77,11 +77,34 @@ def test_material_index_uses_last_shape_and_culls_nothing():
     assert len(np.unique(a)) > 10
 
 
-def test_more_than_256_materials_is_rejected():
-    from diaphane_gb300 import DiaphaneError, Material, Shape
-    scene = Scene.empty(Extent.cube(12), 1e-3).with_boundary(__import__("diaphane_gb300").Boundary.PEC)
-    for i in range(300):
-        scene.materials.push(Material.dielectric(1.0 + 0.01 * i))
+def many_materials(count, side=20):
+    """`count` materials, each painted on its own small cube somewhere in the grid."""
+    from diaphane_gb300 import Boundary, Material, Shape
+    scene = Scene.empty(Extent.cube(side), 1e-3).with_boundary(Boundary.PEC)
+    for i in range(count - 1):
+        m = scene.materials.push(Material.dielectric(1.5 + 0.001 * i))
+        x, y, z = (i * 7) % side, (i * 11) % side, (i * 13) % side
+        centre = [(c - side / 2 + 0.5) * 1e-3 for c in (x, y, z)]
+        scene.shapes.append(Shape.block(centre, (1e-3, 1e-3, 1e-3), m))
+    return scene
+
+
+def test_past_256_materials_the_index_widens_to_u16():
+    scene = many_materials(300)
+    resolved = ResolvedScene(scene)
+    assert resolved.index_bytes == 2 and resolved.material_count == 300
+    ours = resolved.table(_abi.DP_TABLE_MATERIAL_INDEX)
+    assert ours.dtype == np.uint16
+    theirs = oracle.OracleSimulation(scene).table(_abi.DP_TABLE_MATERIAL_INDEX)
+    assert np.array_equal(ours.astype(np.uint32), theirs)
+    assert ours.max() > 255
+
+
+def test_more_than_65536_materials_is_rejected():
+    from diaphane_gb300 import Boundary, DiaphaneError, Material
+    scene = Scene.empty(Extent.cube(4), 1e-3).with_boundary(Boundary.PEC)
+    # 65537 distinct entries (pushing them one by one would merge-check each).
+    scene.materials.materials += [Material.dielectric(1.0 + 1e-5 * (i + 1)) for i in range(65536)]
     with pytest.raises(DiaphaneError) as err:
         ResolvedScene(scene)
     assert err.value.name == "DP_ERR_UNSUPPORTED"
