@@ -164,6 +164,10 @@ SIGNATURES = [
     ("dp_sim_row_pitch", C.c_uint32, [_P]),
     ("dp_sim_launch_count", C.c_uint64, [_P]),
     ("dp_scene_raster", C.c_int, [_P, _P, C.c_uint32, _P]),
+    ("dp_scene_cell_lookup", C.c_int, [_P, C.c_uint32, _P, C.c_size_t]),
+    ("dp_scene_lookup_samples", C.c_uint32, [_P]),
+    ("dp_sim_energy_density", C.c_int, [_P, _P, C.c_size_t]),
+    ("dp_sim_sample", C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
     ("dp_sim_set_probes", C.c_int, [_P, _P, C.c_uint32, C.c_uint64]),
     ("dp_sim_read_probes", C.c_int, [_P, C.c_uint64, C.c_uint64, _P, C.c_size_t]),
     ("dp_sim_read_field_async", C.c_int, [_P, C.c_uint32, _P, C.c_size_t]),

@@ -117,6 +117,21 @@ dp_status dp_scene_info_get(const dp_scene *scene, dp_scene_info *out) {
     });
 }
 
+dp_status dp_scene_cell_lookup(const dp_scene *scene, uint32_t samples, float *host, size_t count) {
+    return guarded([&] {
+        if (!scene || !host) throw Error(DP_ERR_INVALID, "null argument");
+        const Scene &s = scene->scene;
+        if (samples == 0) samples = s.lookup_samples();
+        if (samples < 2) throw Error(DP_ERR_RANGE, "a lookup needs at least two samples per axis");
+        if (count != 3 * size_t(samples)) throw Error(DP_ERR_RANGE, "count must be 3 × samples");
+        const std::vector<float> lookup = s.cell_lookup(samples);
+        std::copy(lookup.begin(), lookup.end(), host);
+        return DP_OK;
+    });
+}
+
+uint32_t dp_scene_lookup_samples(const dp_scene *scene) { return scene ? scene->scene.lookup_samples() : 0; }
+
 dp_status dp_scene_table(const dp_scene *scene, uint32_t table, void *host, size_t bytes) {
     return guarded([&] {
         if (!scene || !host) throw Error(DP_ERR_INVALID, "null argument");

@@ -93,6 +93,7 @@ void launch_energy(const DeviceScene &s, FieldSet f, const float *primary, const
 void launch_energy(const DeviceScene &s, FieldSet64 f, const float *primary, const float *dual,
                    const float2 *eps_mu, double *partials, uint32_t blocks, cudaStream_t stream);
 void launch_finite(const DeviceScene &s, FieldSet f, int32_t *flag, cudaStream_t stream);
+void launch_energy_density(const DeviceScene &s, FieldSet f, float *dense_out, cudaStream_t stream);
 uint32_t energy_blocks(uint64_t cells);
 
 // Fused path (kernels_fused.cu): one launch per step, reads one field set

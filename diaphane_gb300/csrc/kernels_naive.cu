@@ -174,6 +174,22 @@ __global__ void __launch_bounds__(kThreads) energy_pass(DeviceScene s, Fields<T>
     }
 }
 
+// energy_density (src/cpu.rs:689-703): ½(E² + H²) summed over the three
+// components, per cell, into dense rows.
+__global__ void __launch_bounds__(kThreads) energy_density_pass(DeviceScene s, FieldSet f, float *__restrict__ out) {
+    const uint64_t dense = uint64_t(s.n[0]) * s.n[1] * s.n[2];
+    const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
+    if (i >= dense) return;
+    const uint64_t at = (i / s.n[0]) * s.pitch + i % s.n[0];
+    float density = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float e = f.e[uint64_t(a) * s.cells + at], h = f.h[uint64_t(a) * s.cells + at];
+        density += 0.5f * (e * e + h * h);
+    }
+    out[i] = density;
+}
+
 // is_finite (src/cpu.rs:707-713): any non-finite value clears the flag.
 __global__ void __launch_bounds__(kThreads) finite_pass(DeviceScene s, FieldSet f, int32_t *flag) {
     const uint64_t total = 3 * s.cells;
@@ -249,6 +265,10 @@ void launch_energy(const DeviceScene &s, FieldSet f, const float *primary, const
 void launch_energy(const DeviceScene &s, FieldSet64 f, const float *primary, const float *dual, const float2 *eps_mu,
                    double *partials, uint32_t blocks, cudaStream_t stream) {
     energy_pass<double><<<blocks, kThreads, 0, stream>>>(s, f, primary, dual, eps_mu, partials);
+}
+
+void launch_energy_density(const DeviceScene &s, FieldSet f, float *dense_out, cudaStream_t stream) {
+    energy_density_pass<<<blocks_for(uint64_t(s.n[0]) * s.n[1] * s.n[2]), kThreads, 0, stream>>>(s, f, dense_out);
 }
 
 void launch_finite(const DeviceScene &s, FieldSet f, int32_t *flag, cudaStream_t stream) {

@@ -448,20 +448,10 @@ dp_status dp_renderer_create(dp_sim *sim, uint32_t width, uint32_t height, dp_re
         sim->bind();
         const Scene &s = sim->scene;
         const uint32_t *n = s.grid.n;
-        // Grid::cell_lookup (src/grid.rs:635-646), four samples per coarse
-        // cell of the longest axis (src/gpu.rs:225-228).
-        r->samples = std::min<uint32_t>(std::max<uint32_t>(4 * std::max(std::max(n[0], n[1]), n[2]), 256), 8192);
-        std::vector<float> lookup;
-        lookup.reserve(3 * size_t(r->samples));
-        for (int a = 0; a < 3; ++a) {
-            const Axis1D &axis = s.grid.axes[a];
-            const float length = axis.length();
-            for (uint32_t k = 0; k < r->samples; ++k) {
-                const float fraction = float(k) / float(r->samples - 1);
-                lookup.push_back(axis.coordinate((fraction - 0.5f) * length));
-            }
-            r->box[a] = length / s.grid.base; // Grid::box_size, src/grid.rs:621-623
-        }
+        // The world-to-cell table at the reference GPU solver's sample count.
+        r->samples = s.lookup_samples();
+        const std::vector<float> lookup = s.cell_lookup(r->samples);
+        for (int a = 0; a < 3; ++a) r->box[a] = s.grid.axes[a].length() / s.grid.base; // Grid::box_size
         check_cuda(cudaMalloc(&r->lookup, lookup.size() * sizeof(float)), "lookup");
         check_cuda(cudaMemcpy(r->lookup, lookup.data(), lookup.size() * sizeof(float), cudaMemcpyHostToDevice), "lookup");
         check_cuda(cudaMalloc(&r->image, size_t(width) * height * 4), "image");

@@ -375,6 +375,25 @@ const std::vector<uint8_t> &Scene::material_index() const {
     return index_cache_;
 }
 
+std::vector<float> Scene::cell_lookup(uint32_t samples) const {
+    std::vector<float> lookup;
+    lookup.reserve(3 * size_t(samples));
+    for (int a = 0; a < 3; ++a) {
+        const Axis1D &axis = grid.axes[a];
+        const float length = axis.length();
+        for (uint32_t k = 0; k < samples; ++k) {
+            const float fraction = float(k) / float(samples - 1);
+            lookup.push_back(axis.coordinate((fraction - 0.5f) * length));
+        }
+    }
+    return lookup;
+}
+
+uint32_t Scene::lookup_samples() const {
+    const uint32_t longest = std::max(std::max(grid.n[0], grid.n[1]), grid.n[2]);
+    return std::min<uint32_t>(std::max<uint32_t>(4 * longest, 256), 8192);
+}
+
 Scene Scene::build(const dp_scene_desc &d) {
     Scene s;
     s.grid = ResolvedGrid::build(d.grid);

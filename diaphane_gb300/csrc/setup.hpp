@@ -121,6 +121,12 @@ struct Scene {
     // instead (raster.cu); this copy serves the table export and checks.
     const std::vector<uint8_t> &material_index() const;
     uint32_t index_bytes = 1;
+
+    // Grid::cell_lookup (src/grid.rs:635-646): world position (coarse cells
+    // from the low corner) to fractional cell coordinate, `samples` per axis.
+    std::vector<float> cell_lookup(uint32_t samples) const;
+    // The sample count the reference's GPU solver uses (src/gpu.rs:225-228).
+    uint32_t lookup_samples() const;
     uint32_t axis_offset(int axis) const { return axis == 0 ? 0 : (axis == 1 ? grid.n[0] : grid.n[0] + grid.n[1]); }
 
     // Source::injections for every source at `time`, two slots per source.

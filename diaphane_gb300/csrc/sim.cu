@@ -356,6 +356,39 @@ uint32_t dp_sim_row_pitch(const dp_sim *sim) { return sim ? sim->pitch : 0; }
 
 uint64_t dp_sim_launch_count(const dp_sim *sim) { return sim ? sim->launches : 0; }
 
+dp_status dp_sim_energy_density(dp_sim *sim, float *host, size_t count) {
+    return guarded([&] {
+        if (!sim || !host) throw Error(DP_ERR_INVALID, "null argument");
+        const uint64_t cells = sim->scene.grid.cells();
+        if (count != cells) throw Error(DP_ERR_RANGE, "element count does not match the grid");
+        sim->bind();
+        float *dense = nullptr;
+        check(cudaMallocAsync(reinterpret_cast<void **>(&dense), cells * sizeof(float), sim->stream), "density");
+        launch_energy_density(sim->dev, sim->fields(), dense, sim->stream);
+        ++sim->launches;
+        check(cudaGetLastError(), "density launch");
+        check(cudaMemcpyAsync(host, dense, cells * sizeof(float), cudaMemcpyDeviceToHost, sim->stream), "density");
+        check(cudaFreeAsync(dense, sim->stream), "density");
+        sim->wait(kDefaultTimeoutMs);
+        return DP_OK;
+    });
+}
+
+dp_status dp_sim_sample(dp_sim *sim, uint32_t field, uint32_t axis, const uint32_t coord[3], float *out) {
+    return guarded([&] {
+        if (!sim || !coord || !out) throw Error(DP_ERR_INVALID, "null argument");
+        const uint32_t *n = sim->scene.grid.n;
+        if (coord[0] >= n[0] || coord[1] >= n[1] || coord[2] >= n[2]) throw Error(DP_ERR_RANGE, "cell outside the grid");
+        if (axis > 2 || (field == DP_FIELD_INTENSITY && axis != 0)) throw Error(DP_ERR_RANGE, "no such component");
+        const uint64_t at = (uint64_t(coord[2]) * n[1] + coord[1]) * sim->pitch + coord[0];
+        const float *src = field_ptr(sim, field) + uint64_t(axis) * sim->padded_cells() + at;
+        sim->bind();
+        check(cudaMemcpyAsync(out, src, sizeof(float), cudaMemcpyDeviceToHost, sim->stream), "sample");
+        sim->wait(kDefaultTimeoutMs);
+        return DP_OK;
+    });
+}
+
 dp_status dp_sim_read_field_async(dp_sim *sim, uint32_t field, float *host, size_t count) {
     return guarded([&] {
         if (!sim || !host) throw Error(DP_ERR_INVALID, "null argument");

@@ -71,6 +71,16 @@ class ResolvedScene:
         on `stream`."""
         _abi.check(_abi.lib().dp_scene_raster(self.handle, C.c_void_p(device_ptr), row_pitch, C.c_void_p(stream)))
 
+    def lookup_samples(self) -> int:
+        return _abi.lib().dp_scene_lookup_samples(self.handle)
+
+    def cell_lookup(self, samples: int = 0) -> np.ndarray:
+        """Grid::cell_lookup: world-to-cell map, three sections of `samples`."""
+        samples = samples or self.lookup_samples()
+        out = np.empty(3 * samples, np.float32)
+        _abi.check(_abi.lib().dp_scene_cell_lookup(self.handle, samples, out.ctypes.data, out.size))
+        return out
+
     def table(self, which: int) -> np.ndarray:
         span = sum(self.extent)
         sizes = {
@@ -201,6 +211,23 @@ class Simulation:
         e, m = C.c_double(), C.c_double()
         _abi.check(_abi.lib().dp_sim_energy(self.handle, C.byref(e), C.byref(m)))
         return Energy(e.value, m.value)
+
+    def energy_density(self) -> np.ndarray:
+        out = np.empty(self.cells, np.float32)
+        _abi.check(_abi.lib().dp_sim_energy_density(self.handle, out.ctypes.data, out.size))
+        return out
+
+    def _sample(self, field: int, axis: int, coord) -> float:
+        c = (C.c_uint32 * 3)(*[int(v) for v in coord])
+        out = C.c_float()
+        _abi.check(_abi.lib().dp_sim_sample(self.handle, field, int(axis), c, C.byref(out)))
+        return out.value
+
+    def sample_electric(self, axis: Axis, coord) -> float:
+        return self._sample(_abi.DP_FIELD_ELECTRIC, axis, coord)
+
+    def sample_magnetic(self, axis: Axis, coord) -> float:
+        return self._sample(_abi.DP_FIELD_MAGNETIC, axis, coord)
 
     def is_finite(self) -> bool:
         flag = C.c_int32()

@@ -186,6 +186,14 @@ typedef struct dp_scene_info {
     uint32_t index_bytes;  /* bytes per cell of the material index: 1 up to 256 materials, else 2 */
 } dp_scene_info;
 
+/* Grid::cell_lookup (src/grid.rs:635-646): three sections of `samples` values
+ * (0 = the reference GPU solver's count, dp_scene_lookup_samples), each the
+ * fractional cell coordinate of a uniformly spaced world position — the
+ * renderer's world-to-cell map (gpu::Simulation::lookup_buffer). */
+dp_status dp_scene_cell_lookup(const dp_scene *scene, uint32_t samples, float *host, size_t count);
+/* gpu::Simulation::lookup_samples (src/gpu.rs:225-228, 349-351). */
+uint32_t dp_scene_lookup_samples(const dp_scene *scene);
+
 /* Tables a kernel consumes, readable for parity checks. */
 enum {
     DP_TABLE_MAGNETIC_GAINS = 0, /* f32 nx+ny+nz: Grid::magnetic_gains, src/grid.rs:602-604 */
@@ -380,6 +388,13 @@ dp_status dp_sim_read_probes(dp_sim *sim, uint64_t first_step, uint64_t steps, f
  * stream behind the steps already issued; the host buffer (pinned for true
  * overlap) is valid after dp_sim_wait. */
 dp_status dp_sim_read_field_async(dp_sim *sim, uint32_t field, float *host, size_t count);
+/* cpu::Simulation::energy_density (src/cpu.rs:689-703): ½(E² + H²) per cell,
+ * summed over the three components, in f32. */
+dp_status dp_sim_energy_density(dp_sim *sim, float *host, size_t count);
+/* cpu::Simulation::sample_electric / sample_magnetic (src/cpu.rs:154-161):
+ * one component at one cell (DP_FIELD_INTENSITY with axis 0 reads the
+ * accumulated intensity). */
+dp_status dp_sim_sample(dp_sim *sim, uint32_t field, uint32_t axis, const uint32_t coord[3], float *out);
 
 /* ---- Device keyframes (Timeline, src/timeline.rs:76-213) -----------------
  * A ring of `capacity` field snapshots kept in device memory (24 bytes per

@@ -46,6 +46,7 @@ def lib() -> C.CDLL:
             "or_sim_sample": (C.c_float, [P, C.c_int, C.c_int, C.c_uint32, C.c_uint32, C.c_uint32]),
             "or_sim_component": (C.c_int, [P, C.c_int, C.c_int, P]),
             "or_sim_energy": (None, [P, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+            "or_sim_energy_density": (C.c_int, [P, P]),
             "or_sim_is_finite": (C.c_int, [P]),
             "or_sim_extent": (None, [P, C.POINTER(C.c_uint32)]),
             "or_sim_time_step": (C.c_float, [P]),
@@ -186,6 +187,11 @@ class OracleSimulation:
         e, m = C.c_double(), C.c_double()
         lib().or_sim_energy(self.handle, C.byref(e), C.byref(m))
         return Energy(e.value, m.value)
+
+    def energy_density(self) -> np.ndarray:
+        out = np.empty(self.cells, dtype=np.float32)
+        _check(lib().or_sim_energy_density(self.handle, out.ctypes.data))
+        return out
 
     def is_finite(self) -> bool:
         return bool(lib().or_sim_is_finite(self.handle))

@@ -837,6 +837,19 @@ template <typename T> struct Simulation : SimBase {
         }
     }
 
+    // energy_density — src/cpu.rs:689-703: per cell, summed over both fields.
+    void energy_density(float *out) const {
+        const size_t n = grid.total();
+        for (size_t i = 0; i < n; ++i) {
+            float density = 0.0f;
+            for (int a = 0; a < 3; ++a) {
+                const float e = float(electric[a][i]), h = float(magnetic[a][i]);
+                density += 0.5f * (e * e + h * h);
+            }
+            out[i] = density;
+        }
+    }
+
     // energy — src/cpu.rs:654-687
     void energy(double *electric_out, double *magnetic_out) const {
         const size_t ext[3] = {grid.extent[0], grid.extent[1], grid.extent[2]};
@@ -1053,6 +1066,13 @@ void or_sim_energy(const or_sim *s, double *electric, double *magnetic) {
 }
 
 int or_sim_is_finite(const or_sim *s) { return s->f32 ? s->f32->is_finite() : s->f64->is_finite(); }
+
+// Scene::energy_density of the f32 instance.
+int or_sim_energy_density(const or_sim *s, float *out) {
+    if (!s->f32) return 1;
+    s->f32->energy_density(out);
+    return 0;
+}
 
 void or_sim_extent(const or_sim *s, uint32_t out[3]) {
     const Grid &g = s->f32 ? s->f32->grid : s->f64->grid;

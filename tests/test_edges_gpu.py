@@ -9,7 +9,7 @@ import pytest
 import oracle
 from diaphane_gb300 import (DP_KERNEL_AUTO, DP_KERNEL_FUSED, DP_KERNEL_NAIVE, Axis, Batch, Boundary, DiaphaneError,
                             Extent, Material, ResolvedScene, Scene, Shape, Source, Waveform)
-from diaphane_gb300 import Simulation
+from diaphane_gb300 import Simulation, workloads
 from diaphane_gb300._abi import DP_ERR_UNSUPPORTED
 
 pytestmark = pytest.mark.gpu
@@ -98,3 +98,23 @@ def test_past_256_materials_the_index_widens_and_stays_exact(threads):
     assert np.array_equal(bits(sim.read_magnetic()), bits(ref.read_magnetic()))
     e, m = sim.energy(), ref.energy()
     assert e.total() == pytest.approx(m.total(), rel=1e-9)
+
+
+def test_energy_density_and_samples_match_the_oracle(threads):
+    """cpu::Simulation::energy_density and sample_* (src/cpu.rs:154-161,
+    689-703) on the device."""
+    scene = workloads.mixed_scene(21, lo=30, hi=46)
+    sim = Simulation(scene)
+    sim.set_accumulate_intensity(True)
+    ref = oracle.OracleSimulation(scene, threads=threads)
+    ref.set_accumulate_intensity(True)
+    sim.advance_by(70)
+    ref.advance_by(70)
+    assert np.array_equal(bits(sim.energy_density()), bits(ref.energy_density()))
+    n = sim.extent
+    for coord in [(0, 0, 0), (n[0] // 2, n[1] // 3, n[2] // 4), (n[0] - 1, n[1] - 1, n[2] - 1)]:
+        for axis in (Axis.X, Axis.Y, Axis.Z):
+            assert np.float32(sim.sample_electric(axis, coord)) == np.float32(ref.sample_electric(axis, coord))
+            assert np.float32(sim.sample_magnetic(axis, coord)) == np.float32(ref.sample_magnetic(axis, coord))
+    with pytest.raises(DiaphaneError):
+        sim.sample_electric(Axis.X, (n[0], 0, 0))

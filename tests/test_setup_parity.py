@@ -108,3 +108,23 @@ def test_more_than_65536_materials_is_rejected():
     with pytest.raises(DiaphaneError) as err:
         ResolvedScene(scene)
     assert err.value.name == "DP_ERR_UNSUPPORTED"
+
+
+@pytest.mark.parametrize("case", ["graded", "photon"])
+def test_world_to_cell_lookup_matches_the_oracles_coordinate_map(case):
+    """Grid::cell_lookup (src/grid.rs:635-646) against the oracle's own
+    world-to-cell map, sample for sample."""
+    scene = scenes.graded()[0] if case == "graded" else scenes.photon()[0]
+    resolved = ResolvedScene(scene)
+    samples = resolved.lookup_samples()
+    assert samples == min(max(4 * max(resolved.extent), 256), 8192)
+    ours = resolved.cell_lookup()
+    size = oracle.grid_resolve(scene.grid)["size"]
+    expected = np.empty(3 * samples, np.float32)
+    for k in range(samples):
+        fraction = np.float32(k) / np.float32(samples - 1)
+        position = [(fraction - np.float32(0.5)) * np.float32(size[a]) for a in range(3)]
+        cell = oracle.grid_map(scene.grid, _abi.DP_MAP_TO_CELL, position)
+        for a in range(3):
+            expected[a * samples + k] = cell[a]
+    assert np.array_equal(ours.view(np.uint32), expected.view(np.uint32))
