@@ -391,11 +391,23 @@ def batched_measurement(scene_count: int, steps: int, device: int = 0, rank: int
     batch = Batch(arena, chunk_steps=50, max_scenes=max(1, len(resolved)), device=device)
     t0 = time.perf_counter()
     ids = [batch.add(r, steps) for r in resolved]
+    batch.wait()
+    t1 = time.perf_counter()
     batch.run_to_completion()
+    t2 = time.perf_counter()
     outs = [batch.read_electric(i) for i in ids]
-    batched_s = max_over_ranks(time.perf_counter() - t0, world)
+    t3 = time.perf_counter()
+    batched_s = max_over_ranks(t3 - t0, world)
+    stepping_s = max_over_ranks(t2 - t1, world)
     identical = all(np.array_equal(outs[k].view(np.uint32), plain_out[k].view(np.uint32)) for k in plain_out)
+    peak, peak_kind = measured_peaks()
+    step_gbs = BYTES_PER_CELL * cells * steps / stepping_s / 1e9
     return {"scenes": scene_count, "steps": steps, "cells": cells,
+            "phases_s": {"add": t1 - t0, "stepping": t2 - t1, "read": t3 - t2},
+            "stepping_roofline": {"bound": "hbm", "achieved": step_gbs, "peak": peak, "unit": "GB/s",
+                                  "frac": step_gbs / peak, "peak_kind": peak_kind,
+                                  "what": "48 B per cell-update over the stepping phase's wall clock "
+                                          "(graph replays, staging and launches included)"},
             "batched_solves_per_s": scene_count / batched_s, "plain_solves_per_s": scene_count / plain_s,
             "speedup": plain_s / batched_s, "batched_gcells": cells * steps / batched_s / 1e9,
             "plain_gcells": cells * steps / plain_s / 1e9, "batched_s": batched_s, "plain_s": plain_s,
