@@ -356,6 +356,20 @@ uint32_t dp_sim_row_pitch(const dp_sim *sim) { return sim ? sim->pitch : 0; }
 
 uint64_t dp_sim_launch_count(const dp_sim *sim) { return sim ? sim->launches : 0; }
 
+// Not in the public header: raises the error flag a fused step sets when one
+// of its bounded waits gives up, so the test suite can check how the host
+// reports it without making any wait on the GPU run out.
+dp_status dp_internal_raise_wait_error(dp_sim *sim) {
+    return guarded([&] {
+        if (!sim) throw Error(DP_ERR_INVALID, "null handle");
+        sim->bind();
+        const int32_t one = 1;
+        check(cudaMemcpyAsync(sim->error, &one, sizeof(one), cudaMemcpyHostToDevice, sim->stream), "error flag");
+        check(cudaStreamSynchronize(sim->stream), "error flag");
+        return DP_OK;
+    });
+}
+
 dp_status dp_sim_energy_density(dp_sim *sim, float *host, size_t count) {
     return guarded([&] {
         if (!sim || !host) throw Error(DP_ERR_INVALID, "null argument");

@@ -118,3 +118,26 @@ def test_energy_density_and_samples_match_the_oracle(threads):
             assert np.float32(sim.sample_magnetic(axis, coord)) == np.float32(ref.sample_magnetic(axis, coord))
     with pytest.raises(DiaphaneError):
         sim.sample_electric(Axis.X, (n[0], 0, 0))
+
+
+def test_a_wait_that_gave_up_is_reported_once_and_the_handle_stays_usable(threads):
+    """A fused step whose bounded ring wait runs out sets an error flag and
+    returns; the next wait reports DP_ERR_TIMEOUT and clears it.  The flag is
+    raised from the host here, so no wait on the GPU is made to run out."""
+    import ctypes as C
+    from diaphane_gb300 import _abi
+    from diaphane_gb300._abi import DP_ERR_TIMEOUT
+    fn = _abi.lib().dp_internal_raise_wait_error
+    fn.restype, fn.argtypes = C.c_int, [C.c_void_p]
+    scene = small_scene((24, 20, 16))
+    sim = Simulation(scene, kernel=DP_KERNEL_FUSED)
+    sim.advance_by(5)
+    assert fn(sim.handle) == 0
+    with pytest.raises(DiaphaneError) as err:
+        sim.wait()
+    assert err.value.status == DP_ERR_TIMEOUT
+    sim.wait()  # reported once
+    sim.advance_by(10)
+    ref = oracle.OracleSimulation(scene, threads=threads)
+    ref.advance_by(15)
+    assert np.array_equal(bits(sim.read_electric()), bits(ref.read_electric()))
