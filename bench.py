@@ -55,7 +55,7 @@ def parse():
     p.add_argument("--variant", default="", help="fused kernel cx,tile_y,slots (default: tuned)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the mixed-size batch measurement")
-    p.add_argument("--workload", choices=["heterogeneous", "batched", "served", "accuracy"], default="heterogeneous")
+    p.add_argument("--workload", choices=["heterogeneous", "batched", "served", "accuracy", "extras"], default="heterogeneous")
     p.add_argument("--scenes", type=int, default=256, help="batched: scenes per batch")
     p.add_argument("--batch-steps", type=int, default=1000, help="batched: steps per scene")
     p.add_argument("--rates", default="4,16,64", help="served: arrival rates to sweep, requests/s")
@@ -529,6 +529,91 @@ def drift_case(device: int = 0, early: int = 400, late: int = 20_000, window: in
     return out
 
 
+def extras_measurement(side: int = 256, device: int = 0) -> dict:
+    """The costs of the paths around the step, on the heterogeneous scene:
+    scene rasterization (device against host), a backward scrub with the
+    keyframes in device memory against keyframes on the host, a rendered
+    frame, and the probe gather's per-step cost.  Wall clock, synchronized."""
+    import numpy as np
+    import torch
+    from diaphane_gb300 import DeviceTimeline, ResolvedScene, Simulation, Timeline, _abi, workloads
+    from diaphane_gb300.render import Renderer, View
+    out = {"side": side}
+    scene = workloads.heterogeneous(side)
+    resolved = ResolvedScene(scene)
+    # Rasterization: the u8 index on the device vs the host rasterizer (all cores).
+    buf = torch.empty(resolved.cells, dtype=torch.uint8, device=f"cuda:{device}")
+    resolved.rasterize(buf.data_ptr())
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for _ in range(5):
+        resolved.rasterize(buf.data_ptr())
+    torch.cuda.synchronize(device)
+    device_ms = (time.perf_counter() - t0) / 5 * 1e3
+    t0 = time.perf_counter()
+    host = ResolvedScene(scene).table(_abi.DP_TABLE_MATERIAL_INDEX)
+    host_ms = (time.perf_counter() - t0) * 1e3
+    out["raster"] = {"device_ms": device_ms, "host_ms_including_setup": host_ms, "host_threads": os.cpu_count(),
+                     "identical": bool(np.array_equal(buf.cpu().numpy(), host)), "shapes": len(scene.shapes)}
+    del buf
+    # Scrubbing: 10 keyframes 20 steps apart, then seeks back to 15 targets.
+    sims = {}
+    for kind in ("device", "host"):
+        sim = Simulation(resolved, device=device)
+        tl = DeviceTimeline(sim, 20, 10) if kind == "device" else Timeline(20, 10)
+        for _ in range(40):
+            sim.advance_by(5)
+            tl.observe(sim)
+        sim.wait()
+        # Each target lies one step past a keyframe and below the last one,
+        # so every seek restores a keyframe and replays a single step.
+        targets = [181, 161, 141, 121, 101, 81, 61, 41, 21]
+        t0 = time.perf_counter()
+        for target in targets:
+            outcome = tl.seek(sim, target)
+            assert outcome.kind == "keyframe" and outcome.replayed == 1, outcome
+            sim.wait()
+        seek_ms = (time.perf_counter() - t0) / len(targets) * 1e3
+        sims[kind] = (sim, tl)
+        out[f"scrub_{kind}_keyframes_ms"] = seek_ms
+    out["scrub_note"] = ("mean wall time of 9 backward seeks, each restoring a keyframe and replaying one "
+                         "step; keyframes every 20 steps, 24 B per cell each")
+    same = np.array_equal(sims["device"][0].read_electric().view(np.uint32),
+                          sims["host"][0].read_electric().view(np.uint32))
+    out["scrub_identical"] = bool(same)
+    sim, device_timeline = sims["device"]
+    del sims
+    # A frame of the E-and-H view at 1280x720.
+    renderer = Renderer(sim, 1280, 720)
+    renderer.measure()
+    renderer.draw(View())
+    sim.wait()
+    t0 = time.perf_counter()
+    for k in range(10):
+        renderer.draw(View(yaw=0.9 + 0.05 * k))
+    sim.wait()
+    out["render_ms_per_frame"] = (time.perf_counter() - t0) / 10 * 1e3
+    out["render_size"] = [1280, 720]
+    # Probes: 8 cells recorded every step.
+    stream = torch.cuda.ExternalStream(sim_stream(sim), device=device)
+    def timed(steps):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        sim.advance_by(steps)
+        b.record(stream)
+        sim.wait()
+        return a.elapsed_time(b) / steps
+    # The same 60 steps from the same keyframe, without and then with probes.
+    device_timeline.seek(sim, 100)
+    plain = timed(60)
+    device_timeline.seek(sim, 100)
+    sim.set_probes([(side // 2, side // 2, k * side // 8) for k in range(8)], 1024)
+    probed = timed(60)
+    out["probe_us_per_step"] = (probed - plain) * 1e3
+    out["step_ms"] = plain
+    return out
+
+
 def run_accuracy(args):
     from diaphane_gb300 import workloads
     cases = [accuracy_case("free flight 80^3", workloads.free_flight(80), 1000),
@@ -549,6 +634,10 @@ def main():
         run_served(args)
     elif args.workload == "accuracy":
         run_accuracy(args)
+    elif args.workload == "extras":
+        line = {"metric": "costs around the step", "workload": "extras"}
+        line.update(extras_measurement(args.side if args.side != 512 else 256))
+        print(json.dumps(line), flush=True)
     else:
         run_ours(args)
 
