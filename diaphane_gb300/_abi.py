@@ -110,6 +110,11 @@ DP_VIEW_ENERGY, DP_VIEW_ELECTRIC, DP_VIEW_MAGNETIC, DP_VIEW_MAGNITUDE = 0, 1, 2,
 DP_VIEW_FIELDS, DP_VIEW_GRID, DP_VIEW_RIBBONS, DP_VIEW_INTENSITY = 4, 5, 6, 7
 
 
+class dp_tuning(C.Structure):
+    _fields_ = [("cells_per_lane", C.c_uint32), ("tile_y", C.c_uint32), ("ring_slots", C.c_uint32),
+                ("z_chunk", C.c_uint32), ("ms_per_step", C.c_float), ("candidates", C.c_uint32)]
+
+
 class dp_seek(C.Structure):
     _fields_ = [("kind", C.c_uint32), ("replayed", C.c_uint64), ("at", C.c_uint64)]
 
@@ -168,6 +173,7 @@ SIGNATURES = [
     ("dp_scene_lookup_samples", C.c_uint32, [_P]),
     ("dp_sim_energy_density", C.c_int, [_P, _P, C.c_size_t]),
     ("dp_sim_sample", C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
+    ("dp_sim_autotune", C.c_int, [_P, C.c_uint32, C.POINTER(dp_tuning)]),
     ("dp_sim_set_probes", C.c_int, [_P, _P, C.c_uint32, C.c_uint64]),
     ("dp_sim_read_probes", C.c_int, [_P, C.c_uint64, C.c_uint64, _P, C.c_size_t]),
     ("dp_sim_read_field_async", C.c_int, [_P, C.c_uint32, _P, C.c_size_t]),

@@ -477,7 +477,7 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
     return guarded([&] {
         if (!b || !scene || !id || (probe_count && !probes)) throw Error(DP_ERR_INVALID, "null argument");
         const Scene &s = scene_of(scene);
-        if (!tensor_maps_available()) throw Error(DP_ERR_UNSUPPORTED, "the driver offers no tensor-map encoder");
+        if (!tensor_maps_available()) throw Error(DP_ERR_UNSUPPORTED, "the CUDA driver offers no tensor-map encoder");
         if (2 * s.sources.size() > size_t(kBatchInjections))
             throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 4 sources");
         if (s.index_bytes != 1) throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 256 materials");

@@ -238,6 +238,14 @@ class Simulation:
     def snapshot(self) -> Snapshot:
         return Snapshot(self.step_count(), self.read_electric(), self.read_magnetic())
 
+    def autotune(self, steps: int = 8) -> dict:
+        """Times each fused-step plan from the current state and keeps the
+        fastest; the state is restored exactly."""
+        t = _abi.dp_tuning()
+        _abi.check(_abi.lib().dp_sim_autotune(self.handle, steps, C.byref(t)))
+        return {"cells_per_lane": t.cells_per_lane, "tile_y": t.tile_y, "ring_slots": t.ring_slots,
+                "z_chunk": t.z_chunk, "ms_per_step": t.ms_per_step, "candidates": t.candidates}
+
     # -- probes and asynchronous read-back ---------------------------------------
     def set_probes(self, cells, capacity: int) -> None:
         """Ez and Hy at `cells` ((x, y, z) each) after every step, kept for the

@@ -375,6 +375,19 @@ uint32_t dp_sim_kernel(const dp_sim *sim);
 /* Kernel launches issued by this handle so far (every kernel of this library). */
 uint64_t dp_sim_launch_count(const dp_sim *sim);
 
+/* ---- Autotuning ---------------------------------------------------------
+ * Times every fused-step tile shape (cells per lane × rows per tile, with its
+ * ring depth) at several z-chunk depths, `steps` steps each (0 = 8), from the
+ * simulation's current state, and keeps the fastest.  The fields, intensity
+ * and step count are restored exactly, so tuning changes no result.  On the
+ * one-thread-per-cell path there is nothing to tune (candidates = 0). */
+typedef struct dp_tuning {
+    uint32_t cells_per_lane, tile_y, ring_slots, z_chunk; /* the chosen plan */
+    float ms_per_step;                                    /* its time per step in the trial */
+    uint32_t candidates;                                  /* plans timed */
+} dp_tuning;
+dp_status dp_sim_autotune(dp_sim *sim, uint32_t steps, dp_tuning *out);
+
 /* ---- Probes and asynchronous read-back ----------------------------------
  * Probes record Ez and Hy at given cells after every step into a device ring
  * of `capacity` steps (one small gather launch per step while set); count 0

@@ -141,3 +141,29 @@ def test_a_wait_that_gave_up_is_reported_once_and_the_handle_stays_usable(thread
     ref = oracle.OracleSimulation(scene, threads=threads)
     ref.advance_by(15)
     assert np.array_equal(bits(sim.read_electric()), bits(ref.read_electric()))
+
+
+def test_autotuning_keeps_the_state_and_the_results(threads):
+    """dp_sim_autotune times the fused step's plans from the current state and
+    restores it exactly: the run continues bit-identical to the oracle."""
+    from tests import scenes
+    scene, _ = scenes.graded()
+    sim = Simulation(scene, kernel=DP_KERNEL_FUSED)
+    sim.set_accumulate_intensity(True)
+    sim.advance_by(12)
+    before_e, before_i = sim.read_electric(), sim.read_intensity()
+    tuning = sim.autotune(steps=3)
+    assert tuning["candidates"] >= 4 and tuning["ms_per_step"] > 0
+    assert tuning["cells_per_lane"] in (1, 2, 4) and tuning["tile_y"] in (8, 16)
+    assert sim.step_count() == 12 and sim.accumulated_steps() == 12
+    assert np.array_equal(bits(sim.read_electric()), bits(before_e))
+    assert np.array_equal(bits(sim.read_intensity()), bits(before_i))
+    sim.advance_by(28)
+    ref = oracle.OracleSimulation(scene, threads=threads)
+    ref.set_accumulate_intensity(True)
+    ref.advance_by(40)
+    assert np.array_equal(bits(sim.read_electric()), bits(ref.read_electric()))
+    assert np.array_equal(bits(sim.read_magnetic()), bits(ref.read_magnetic()))
+    assert np.array_equal(bits(sim.read_intensity()), bits(ref.read_intensity()))
+    naive = Simulation(scene, kernel=DP_KERNEL_NAIVE)
+    assert naive.autotune()["candidates"] == 0

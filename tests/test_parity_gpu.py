@@ -1,10 +1,10 @@
 """The CUDA path against the oracle — the reference's parity contract
 (tests/parity.rs) on every scene it uses, tightened.
 
-The reference allows 1e-4 of the all-component peak; the bar here is the
-north-star's 1e-5 after the full step count, and the expectation is stronger
-still: both sides evaluate the same f32 expressions in the same order with no
-FMA contraction and IEEE division, so the fields must be bit-identical.
+The reference allows 1e-4 of the all-component peak; this path is held to
+1e-5 of peak after the full step count, and the expectation is stronger still:
+both sides evaluate the same f32 expressions in the same order with no FMA
+contraction and IEEE division, so the fields must be bit-identical.
 """
 import numpy as np
 import pytest
