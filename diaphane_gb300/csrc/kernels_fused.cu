@@ -554,9 +554,21 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
             const float ez = *e_at(E, 2, hr, cc), ez_r = *e_at(E, 2, hr, cc + 1), ez_up = *e_at(E, 2, hr + 1, cc);
             const float4 c = coeff[M[hr * G::WM + cc + 12]];
             float nx_ = *h_at(H, 0, hr, cc), ny_ = *h_at(H, 1, hr, cc), nz_ = *h_at(H, 2, hr, cc);
-            nx_ = h_full(nx_, (c.w + (hc.ahy + ahz)) + hc.aix, c.z, hc.mgy * (ez_up - ez) - mgz * (ey_n - ey));
-            ny_ = h_full(ny_, (c.w + (hc.aiy + ahz)) + hc.ahx, c.z, mgz * (ex_n - ex) - hc.mgx * (ez_r - ez));
-            nz_ = h_full(nz_, (c.w + (hc.ahy + aiz)) + hc.ahx, c.z, hc.mgx * (ey_r - ey) - hc.mgy * (ex_up - ex));
+            const float lx = (c.w + (hc.ahy + ahz)) + hc.aix, ly = (c.w + (hc.aiy + ahz)) + hc.ahx;
+            const float lz = (c.w + (hc.ahy + aiz)) + hc.ahx;
+            const float cxh = hc.mgy * (ez_up - ez) - mgz * (ey_n - ey);
+            const float cyh = mgz * (ex_n - ex) - hc.mgx * (ez_r - ez);
+            const float czh = hc.mgx * (ey_r - ey) - hc.mgy * (ex_up - ex);
+            constexpr unsigned kHaloMask = (2u << kHaloRowLanes) - 1u; // lanes 0..kHaloRowLanes
+            if (__all_sync(kHaloMask, lx == 0.0f && ly == 0.0f && lz == 0.0f)) {
+                nx_ = nx_ - c.z * cxh;
+                ny_ = ny_ - c.z * cyh;
+                nz_ = nz_ - c.z * czh;
+            } else {
+                nx_ = h_full(nx_, lx, c.z, cxh);
+                ny_ = h_full(ny_, ly, c.z, cyh);
+                nz_ = h_full(nz_, lz, c.z, czh);
+            }
             if (hc.mask) apply_injections_1(inj, s.weights, hc.mask, hc.x, hc.y, p, nx_, ny_, nz_);
             *h_at(H, 0, hr, cc) = nx_;
             *h_at(H, 1, hr, cc) = ny_;
