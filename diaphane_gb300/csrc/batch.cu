@@ -172,8 +172,14 @@ struct dp_batch {
     std::vector<BatchUnit *> units;               // per variant
     std::vector<uint32_t> unit_counts;
     std::vector<Variant> variants;
-    ProbeSlot *probe_slots = nullptr;
+    ProbeSlot *probe_slots = nullptr;             // grouped by variant
     uint32_t probe_count = 0;
+    std::vector<uint32_t> probe_offset, probe_count_v; // each variant's share of probe_slots
+    // One stream per variant: the variants' scenes are disjoint, so within a
+    // chunk their launches form independent chains that may overlap.
+    std::vector<cudaStream_t> lanes;
+    std::vector<cudaEvent_t> joins;
+    cudaEvent_t fork = nullptr;
     int32_t *error = nullptr;
     // Host staging (pinned), double-buffered against in-flight copies.
     BatchScene *h_scenes[2] = {nullptr, nullptr};
@@ -202,6 +208,9 @@ struct dp_batch {
         cudaFree(counts);
         cudaFree(probe_slots);
         cudaFree(error);
+        for (cudaStream_t l : lanes) cudaStreamDestroy(l);
+        for (cudaEvent_t e : joins) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
         cudaFree(arena_base);
         for (int k = 0; k < 2; ++k) {
             cudaFreeHost(h_scenes[k]);
@@ -224,7 +233,7 @@ struct dp_batch {
         unit_counts.clear();
         variants.clear();
         std::vector<std::vector<BatchUnit>> lists;
-        std::vector<ProbeSlot> probes;
+        std::vector<std::vector<ProbeSlot>> probe_lists;
         for (auto &kv : entries) {
             Entry &e = kv.second;
             size_t v = 0;
@@ -232,11 +241,30 @@ struct dp_batch {
             if (v == variants.size()) {
                 variants.push_back(e.variant);
                 lists.emplace_back();
+                probe_lists.emplace_back();
             }
             lists[v].insert(lists[v].end(), e.units.begin(), e.units.end());
             for (uint32_t k = 0; k < e.probe_cells.size(); ++k)
-                probes.push_back(ProbeSlot{e.slot, k, uint32_t(e.probe_cells.size()), e.probe_cells[k], e.probes});
+                probe_lists[v].push_back(
+                    ProbeSlot{e.slot, k, uint32_t(e.probe_cells.size()), e.probe_cells[k], e.probes});
         }
+        std::vector<ProbeSlot> probes;
+        probe_offset.clear();
+        probe_count_v.clear();
+        for (auto &pl : probe_lists) {
+            probe_offset.push_back(uint32_t(probes.size()));
+            probe_count_v.push_back(uint32_t(pl.size()));
+            probes.insert(probes.end(), pl.begin(), pl.end());
+        }
+        while (lanes.size() < variants.size()) {
+            cudaStream_t l = nullptr;
+            cudaEvent_t j = nullptr;
+            check(cudaStreamCreateWithFlags(&l, cudaStreamNonBlocking), "lane stream");
+            check(cudaEventCreateWithFlags(&j, cudaEventDisableTiming), "lane event");
+            lanes.push_back(l);
+            joins.push_back(j);
+        }
+        if (!fork) check(cudaEventCreateWithFlags(&fork, cudaEventDisableTiming), "fork event");
         for (auto &list : lists) {
             BatchUnit *d = nullptr;
             check(cudaMalloc(&d, std::max<size_t>(1, list.size()) * sizeof(BatchUnit)), "cudaMalloc units");
@@ -262,20 +290,28 @@ struct dp_batch {
         dirty = false;
     }
 
-    // The launches of one chunk reading staging half `half`.
+    // The launches of one chunk reading staging half `half`: one chain per
+    // variant (its steps and its scenes' probe gathers, in order) on that
+    // variant's stream, forked from and joined back into the batch stream.
     void record_chunk(int half) {
         const DeviceInjection *inj = injections + size_t(half) * injection_span();
         const uint32_t *cnt = counts + size_t(half) * count_span();
-        for (uint32_t t = 0; t < chunk; ++t) {
-            for (size_t v = 0; v < variants.size(); ++v) {
+        check(cudaEventRecord(fork, stream), "fork");
+        for (size_t v = 0; v < variants.size(); ++v) {
+            cudaStream_t lane = lanes[v];
+            check(cudaStreamWaitEvent(lane, fork, 0), "fork");
+            for (uint32_t t = 0; t < chunk; ++t) {
                 launch_batch_step(variants[v].cx, variants[v].tile_y, variants[v].slots, scenes, units[v],
-                                  unit_counts[v], inj, cnt, capacity, t, error, stream);
+                                  unit_counts[v], inj, cnt, capacity, t, error, lane);
                 ++launches;
+                if (probe_count_v[v]) {
+                    gather_probes<<<(probe_count_v[v] + 255) / 256, 256, 0, lane>>>(
+                        scenes, probe_slots + probe_offset[v], probe_count_v[v], t);
+                    ++launches;
+                }
             }
-            if (probe_count) {
-                gather_probes<<<(probe_count + 255) / 256, 256, 0, stream>>>(scenes, probe_slots, probe_count, t);
-                ++launches;
-            }
+            check(cudaEventRecord(joins[v], lane), "join");
+            check(cudaStreamWaitEvent(stream, joins[v], 0), "join");
         }
     }
 
@@ -348,7 +384,9 @@ struct dp_batch {
                     cudaGraphDestroy(graph);
                 }
                 check(cudaGraphLaunch(exec[half], stream), "graph launch");
-                launches += uint64_t(chunk) * (variants.size() + (probe_count ? 1 : 0));
+                uint64_t per_step = variants.size();
+                for (uint32_t c : probe_count_v) per_step += c ? 1 : 0;
+                launches += uint64_t(chunk) * per_step;
             } else {
                 record_chunk(half);
             }
