@@ -11,8 +11,9 @@
 //     are separated by a barrier; a fused pass cannot be);
 //   * halo recompute: E at the tile's low x column and low y row needs new H
 //     one cell outside the tile, so the CTA recomputes H there from the same
-//     inputs instead of waiting for the neighbouring CTA (each warp takes an
-//     eighth of the halo row and the halo cell of its own row).
+//     inputs instead of waiting for the neighbouring CTA (the TX + TY halo
+//     cells are packed one per lane onto the first warps, so the other warps
+//     skip that step).
 // Each cell's six components are then read once and written once per step:
 // the 48 B/cell of the reference's own accounting (src/gpu.rs:381-388).
 //
@@ -367,23 +368,28 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
     const uint32_t mask_h = has_inj ? injection_mask(inj, true, xl, xl + CX, y) : 0u;
     const uint32_t mask_e = has_inj ? injection_mask(inj, false, xl, xl + CX, y) : 0u;
 
-    // Halo cells: lanes 0..4CX-1 of warp w take cells [4CX·w, 4CX·(w+1)) of
-    // row y0-1 (the Hx, Hz that E at row y0 reads); lane 4CX takes the cell
-    // (x0-1, y) of the warp's own row (the Hy, Hz that E at x0 reads).
-    constexpr int kHaloRowLanes = G::TX / kWarps;
-    const bool halo_lane = lane <= kHaloRowLanes;
+    // Halo cells, packed onto the first warps: halo index i = 32·warp + lane;
+    // i < TX takes cell x0+i of row y0-1 (the Hx, Hz that E at row y0 reads),
+    // TX <= i < TX+TY takes cell (x0-1, y0+i-TX) (the Hy, Hz that E at x0
+    // reads).  The remaining warps skip the halo step altogether.
+    constexpr int kHalo = G::TX + kWarps;
+    static_assert(kHalo <= kThreads, "every halo cell needs a thread");
+    const int halo_index = 32 * warp + lane;
+    const bool halo_lane = halo_index < kHalo;
+    const int halo_in_warp = kHalo - 32 * warp; // > 0 on warps holding halo cells
+    const unsigned halo_mask = halo_in_warp >= 32 ? 0xffffffffu : (halo_in_warp > 0 ? (1u << halo_in_warp) - 1u : 0u);
     HaloCell hc{};
     if (halo_lane) {
-        if (lane < kHaloRowLanes) {
+        if (halo_index < G::TX) {
             hc.hr = 0;
-            hc.hc = 4 + kHaloRowLanes * warp + lane;
-            hc.x = x0 + kHaloRowLanes * warp + lane;
+            hc.hc = 4 + halo_index;
+            hc.x = x0 + halo_index;
             hc.y = y0 - 1;
         } else {
-            hc.hr = row;
+            hc.hr = halo_index - G::TX + 1;
             hc.hc = 3;
             hc.x = x0 - 1;
-            hc.y = y;
+            hc.y = y0 + (halo_index - G::TX);
         }
         hc.mgx = ldg_at(s.mgain, hc.x, nx);
         hc.aix = ldg_at(absorb_int, hc.x, nx);
@@ -559,8 +565,7 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
             const float cxh = hc.mgy * (ez_up - ez) - mgz * (ey_n - ey);
             const float cyh = mgz * (ex_n - ex) - hc.mgx * (ez_r - ez);
             const float czh = hc.mgx * (ey_r - ey) - hc.mgy * (ex_up - ex);
-            constexpr unsigned kHaloMask = (2u << kHaloRowLanes) - 1u; // lanes 0..kHaloRowLanes
-            if (__all_sync(kHaloMask, lx == 0.0f && ly == 0.0f && lz == 0.0f)) {
+            if (__all_sync(halo_mask, lx == 0.0f && ly == 0.0f && lz == 0.0f)) {
                 nx_ = nx_ - c.z * cxh;
                 ny_ = ny_ - c.z * cyh;
                 nz_ = nz_ - c.z * czh;
