@@ -29,6 +29,9 @@
 // reference's order (src/cpu.rs:323-330, 422-429), compiled without FMA
 // contraction; a cell whose total loss is exactly zero takes the shortcut
 // `h - g*curl`, which is the same IEEE result as `((1-0)h - g*curl)/(1+0)`.
+// A warp in which only a few lanes hold lossy cells (the absorber edge or a
+// lossy slab crossing a tile row) hands their divisions to all 32 lanes
+// through a small per-warp scratch instead of letting every lane divide.
 // Sources are applied to each freshly computed value in the reference's
 // order (src/cpu.rs:606-633), halo cells included, and intensity is summed
 // from the final E (src/cpu.rs:186-196).  The result is bit-identical to the
@@ -71,7 +74,11 @@ template <int CX, int TY, int SLOTS> struct Geometry {
     static constexpr int TX_BYTES = E_BYTES + H_BYTES + M_BYTES; // bytes TMA lands per slot
     static constexpr int COEFF_OFF = kSlots * SLOT;
     static constexpr int BAR_OFF = COEFF_OFF + kMaxMaterials * 16;
-    static constexpr int SMEM = BAR_OFF + kSlots * 8;
+    // Per warp: numerators and denominators of a compacted division.
+    static constexpr int kCompactItems = CX == 1 ? 64 : 96;
+    static constexpr int SCRATCH_OFF = (BAR_OFF + kSlots * 8 + 15) & ~15;
+    static constexpr int SCRATCH_WARP = 2 * kCompactItems * 4;
+    static constexpr int SMEM = SCRATCH_OFF + kWarps * SCRATCH_WARP;
 };
 
 struct FusedArgs {
@@ -208,6 +215,49 @@ __device__ __forceinline__ float ldg_at(const float *base, int i, int n) {
 // is what the fast path below computes; either form is exact for l = 0.
 __device__ __forceinline__ float h_full(float h, float loss, float gain, float curl) {
     return exact_div((1.0f - loss) * h - gain * curl, 1.0f + loss);
+}
+
+// The division step of a warp in which only a few lanes hold lossy cells.
+// Those lanes put their 3·CX numerators and denominators in the warp's
+// scratch, all 32 lanes divide them (one item each per round), and each lossy
+// lane reads its quotients back: ceil(items / 32) divisions per lane instead
+// of 3·CX.  A quotient is the same correctly rounded value whichever lane
+// computes it.  The lossless lanes' numerators are already their results
+// (their denominators are exactly 1).
+template <int CX>
+__device__ __forceinline__ void divide_compacted(float *scratch, int items_max, unsigned lossy_lanes, int lane,
+                                                 bool lossy, Vec<CX> &n0, Vec<CX> &n1, Vec<CX> &n2,
+                                                 const float (&l0)[CX], const float (&l1)[CX],
+                                                 const float (&l2)[CX]) {
+    constexpr int K = 3 * CX;
+    float *num = scratch, *den = scratch + items_max;
+    const int rank = __popc(lossy_lanes & ((1u << lane) - 1u));
+    if (lossy) {
+        Vec<CX> d0, d1, d2;
+#pragma unroll
+        for (int j = 0; j < CX; ++j) {
+            d0.v[j] = 1.0f + l0[j];
+            d1.v[j] = 1.0f + l1[j];
+            d2.v[j] = 1.0f + l2[j];
+        }
+        float *n = num + rank * K, *d = den + rank * K;
+        sts<CX>(n, n0);
+        sts<CX>(n + CX, n1);
+        sts<CX>(n + 2 * CX, n2);
+        sts<CX>(d, d0);
+        sts<CX>(d + CX, d1);
+        sts<CX>(d + 2 * CX, d2);
+    }
+    __syncwarp();
+    const int items = __popc(lossy_lanes) * K;
+    for (int i = lane; i < items; i += 32) num[i] = exact_div(num[i], den[i]);
+    __syncwarp();
+    if (lossy) {
+        const float *n = num + rank * K;
+        n0 = lds<CX>(n);
+        n1 = lds<CX>(n + CX);
+        n2 = lds<CX>(n + 2 * CX);
+    }
 }
 
 // Bit k is set when injection k of `magnetic` phase covers row y and any of
@@ -400,6 +450,8 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         hc.mask = has_inj ? injection_mask(inj, true, hc.x, hc.x + 1, hc.y) : 0u;
     }
 
+    float *scratch = reinterpret_cast<float *>(smem + G::SCRATCH_OFF + warp * G::SCRATCH_WARP);
+
     Vec<CX> hx_prev, hy_prev; // new H at plane z-1, this thread's cells
 #pragma unroll
     for (int j = 0; j < CX; ++j) hx_prev.v[j] = hy_prev.v[j] = 0.0f;
@@ -489,7 +541,8 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 lz[j] = (c.w + row_z) + ahx.v[j];
                 lossless = lossless && lx[j] == 0.0f && ly[j] == 0.0f && lz[j] == 0.0f;
             }
-            if (__all_sync(0xffffffffu, lossless)) {
+            const unsigned lossy_lanes = __ballot_sync(0xffffffffu, !lossless);
+            if (lossy_lanes == 0) {
 #pragma unroll
                 for (int j = 0; j < CX; ++j) {
                     nhx.v[j] = nhx.v[j] - gain[j] * cx_[j];
@@ -516,6 +569,15 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                         nhy.v[j] = n1[j];
                         nhz.v[j] = n2[j];
                     }
+                } else if (__popc(lossy_lanes) * 3 * CX <= G::kCompactItems) {
+#pragma unroll
+                    for (int j = 0; j < CX; ++j) {
+                        nhx.v[j] = n0[j];
+                        nhy.v[j] = n1[j];
+                        nhz.v[j] = n2[j];
+                    }
+                    divide_compacted<CX>(scratch, G::kCompactItems, lossy_lanes, lane, !lossless, nhx, nhy, nhz, lx,
+                                         ly, lz);
                 } else if (__all_sync(0xffffffffu, normal)) {
 #pragma unroll
                     for (int j = 0; j < CX; ++j) {
@@ -609,7 +671,8 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 lossless = lossless && lx[j] == 0.0f && ly[j] == 0.0f && lz[j] == 0.0f;
             }
             Vec<CX> nex, ney, nez;
-            if (__all_sync(0xffffffffu, lossless)) {
+            const unsigned lossy_lanes = __ballot_sync(0xffffffffu, !lossless);
+            if (lossy_lanes == 0) {
 #pragma unroll
                 for (int j = 0; j < CX; ++j) {
                     nex.v[j] = ex.v[j] + ecoef[j].x * cx_[j];
@@ -636,6 +699,15 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                         ney.v[j] = n1[j];
                         nez.v[j] = n2[j];
                     }
+                } else if (__popc(lossy_lanes) * 3 * CX <= G::kCompactItems) {
+#pragma unroll
+                    for (int j = 0; j < CX; ++j) {
+                        nex.v[j] = n0[j];
+                        ney.v[j] = n1[j];
+                        nez.v[j] = n2[j];
+                    }
+                    divide_compacted<CX>(scratch, G::kCompactItems, lossy_lanes, lane, !lossless, nex, ney, nez, lx,
+                                         ly, lz);
                 } else if (__all_sync(0xffffffffu, normal)) {
 #pragma unroll
                     for (int j = 0; j < CX; ++j) {
