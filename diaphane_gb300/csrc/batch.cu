@@ -95,7 +95,8 @@ struct Variant {
 
 // The variant a grid shape runs: the requested tile width, or else the widest
 // tile that wastes no more lanes than a narrower one; 8 rows, and the ring
-// depth that variant is built with.
+// depth that variant is built with (3 slots for 128- and 64-wide tiles, 4 for
+// 32-wide ones, the depths that let 2, 3 and 4 CTAs share an SM).
 Variant variant_for(uint32_t nx, uint32_t requested_cx) {
     uint32_t best = 4, waste_best = ~0u;
     for (uint32_t cx : {4u, 2u, 1u}) {
@@ -106,7 +107,7 @@ Variant variant_for(uint32_t nx, uint32_t requested_cx) {
         }
     }
     if (requested_cx) best = requested_cx;
-    return Variant{best, 8, best == 4 ? 3u : 5u};
+    return Variant{best, 8, best == 1 ? 4u : 3u};
 }
 
 struct Entry {

@@ -784,8 +784,18 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
 // A batch: block b is unit b of this variant's work list.  Scene descriptors
 // (with their tensor maps) live in global memory; a scene that has finished
 // its steps for this chunk, or has left the batch, is skipped.
+// CTAs per SM the batch kernel is built for.  Narrow tiles give each warp
+// few cells per plane, so their fixed per-plane latency (ring waits,
+// barriers, the division chain) is hidden only by more resident warps: the
+// 64-wide form (3-slot ring, 80 registers) fits 3 CTAs per SM and the 32-wide
+// form (4-slot ring, 64 registers) 4, measured 14 % faster on a batch of
+// mixed small scenes than 2 CTAs of each.
+constexpr int batch_blocks(int CX, int TY, int SLOTS) {
+    return CX == 1 && SLOTS <= 4 ? 4 : (CX == 2 && SLOTS <= 3 ? 3 : 16 / TY);
+}
+
 template <int CX, int TY, int SLOTS>
-__global__ void __launch_bounds__(32 * TY, 16 / TY)
+__global__ void __launch_bounds__(32 * TY, batch_blocks(CX, TY, SLOTS))
 fused_batch_step(const BatchScene *__restrict__ scenes, const BatchUnit *__restrict__ units,
                  const DeviceInjection *__restrict__ injections, const uint32_t *__restrict__ injection_counts,
                  uint32_t scene_count, uint32_t step, int32_t *error) {
@@ -991,9 +1001,8 @@ void launch_batch_variant(const BatchScene *scenes, const BatchUnit *units, uint
 
 void configure_batch_kernels() {
     configure_batch_variant<4, 8, 3>();
-    configure_batch_variant<2, 8, 5>();
-    configure_batch_variant<4, 16, 3>();
-    configure_batch_variant<1, 8, 5>();
+    configure_batch_variant<2, 8, 3>();
+    configure_batch_variant<1, 8, 4>();
 }
 
 bool tensor_maps_available() { return encoder() != nullptr; }
@@ -1005,12 +1014,12 @@ void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, const Batch
     if (unit_count == 0) return;
     if (cx == 4 && tile_y == 8 && slots == 3)
         launch_batch_variant<4, 8, 3>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
-    else if (cx == 2 && tile_y == 8 && slots == 5)
-        launch_batch_variant<2, 8, 5>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
-    else if (cx == 4 && tile_y == 16 && slots == 3)
-        launch_batch_variant<4, 16, 3>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
+    else if (cx == 2 && tile_y == 8 && slots == 3)
+        launch_batch_variant<2, 8, 3>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
+    else if (cx == 1 && tile_y == 8 && slots == 4)
+        launch_batch_variant<1, 8, 4>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
     else
-        launch_batch_variant<1, 8, 5>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
+        throw std::runtime_error("no batch kernel variant with that tile shape and ring depth");
 }
 
 void launch_fused_step(const DeviceScene &s, const FusedPlan &plan, const FusedMaps &in_maps, FieldSet out,
