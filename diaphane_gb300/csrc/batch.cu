@@ -456,7 +456,9 @@ void make_units(Entry &e, uint32_t planes) {
     const uint32_t tiles_x = (n[0] + tx - 1) / tx, tiles_y = (n[1] + ty - 1) / ty;
     // Units of `planes` planes (at least 8): enough to amortize a unit's
     // start-up (one extra H plane, ring fill), few enough to spread a scene.
-    const uint32_t depth = std::max<uint32_t>(8, std::min<uint32_t>(planes, n[2]));
+    const uint32_t target = std::max<uint32_t>(8, std::min<uint32_t>(planes, n[2]));
+    const uint32_t chunks = (n[2] + target - 1) / target;
+    const uint32_t depth = (n[2] + chunks - 1) / chunks; // equal chunks, none left short
     e.units.clear();
     for (uint32_t z0 = 0; z0 < n[2]; z0 += depth)
         for (uint32_t ty_i = 0; ty_i < tiles_y; ++ty_i)

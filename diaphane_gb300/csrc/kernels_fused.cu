@@ -375,13 +375,6 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
     float4 *coeff = reinterpret_cast<float4 *>(smem + G::COEFF_OFF);
     const uint32_t bar0 = smem_addr(smem + G::BAR_OFF);
 
-    for (int m = threadIdx.x; m < kMaxMaterials; m += kThreads) coeff[m] = __ldg(&s.coeff[m]);
-    if (threadIdx.x == 0) {
-        for (int k = 0; k < kSlots; ++k) mbar_init(bar0 + 8 * k, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-
     // Plane p goes to slot (p - zs) % kSlots; its n-th use of that slot is
     // phase n & 1.
     auto issue = [&](int p) {
@@ -394,8 +387,16 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         tma_load_3d(smem_addr(slot + G::M_OFF), m_map_p, x0 - 16, y0 - 1, p, bar);
     };
     const int last_plane = z1; // E(z1) feeds H(z1-1); past nz it arrives as zeros
-    if (threadIdx.x == 0)
+    // The first planes are requested before the coefficient table is staged,
+    // so the two latencies overlap; the barrier below publishes both the
+    // table and the initialised ring barriers.
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < kSlots; ++k) mbar_init(bar0 + 8 * k, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         for (int p = zs; p <= min(zs + kSlots - 1, last_plane); ++p) issue(p);
+    }
+    for (int m = threadIdx.x; m < kMaxMaterials; m += kThreads) coeff[m] = __ldg(&s.coeff[m]);
+    __syncthreads();
 
     // Per-thread constants: this lane's cells along x, this warp's row.
     const int row = warp + 1;                // row in the E and H slots
