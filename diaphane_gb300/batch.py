@@ -13,7 +13,7 @@ from typing import Sequence
 import numpy as np
 
 from . import _abi
-from .simulation import ResolvedScene
+from .simulation import ResolvedScene, _output
 
 
 class Batch:
@@ -75,19 +75,19 @@ class Batch:
         _abi.check(_abi.lib().dp_batch_status(self.handle, ident, C.byref(step), C.byref(target)))
         return step.value, target.value
 
-    def _read(self, ident: int, field: int, count: int) -> np.ndarray:
-        out = np.empty(count, dtype=np.float32)
+    def _read(self, ident: int, field: int, count: int, out=None) -> np.ndarray:
+        out = _output(out, count)
         _abi.check(_abi.lib().dp_batch_read_field(self.handle, ident, field, out.ctypes.data, count))
         return out
 
-    def read_electric(self, ident: int) -> np.ndarray:
-        return self._read(ident, _abi.DP_FIELD_ELECTRIC, 3 * self.scenes[ident].cells)
+    def read_electric(self, ident: int, out=None) -> np.ndarray:
+        return self._read(ident, _abi.DP_FIELD_ELECTRIC, 3 * self.scenes[ident].cells, out)
 
-    def read_magnetic(self, ident: int) -> np.ndarray:
-        return self._read(ident, _abi.DP_FIELD_MAGNETIC, 3 * self.scenes[ident].cells)
+    def read_magnetic(self, ident: int, out=None) -> np.ndarray:
+        return self._read(ident, _abi.DP_FIELD_MAGNETIC, 3 * self.scenes[ident].cells, out)
 
-    def read_intensity(self, ident: int) -> np.ndarray:
-        return self._read(ident, _abi.DP_FIELD_INTENSITY, self.scenes[ident].cells)
+    def read_intensity(self, ident: int, out=None) -> np.ndarray:
+        return self._read(ident, _abi.DP_FIELD_INTENSITY, self.scenes[ident].cells, out)
 
     def read_probes(self, ident: int) -> np.ndarray:
         step, _ = self.status(ident)

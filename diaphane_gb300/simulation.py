@@ -19,6 +19,17 @@ from . import _abi
 from .scene import Axis, Scene
 
 
+def _output(out, count: int) -> np.ndarray:
+    """`out` (a contiguous float32 array of at least `count` values, e.g. a view
+    of pinned host memory, which a copy reaches at full link speed) or a new
+    array."""
+    if out is None:
+        return np.empty(count, dtype=np.float32)
+    if out.dtype != np.float32 or not out.flags.c_contiguous or out.size < count:
+        raise ValueError(f"out must be a contiguous float32 array of at least {count} values")
+    return out.reshape(-1)[:count]
+
+
 @dataclass
 class Energy:
     """src/cpu.rs:52-62."""
@@ -164,19 +175,19 @@ class Simulation:
         return _abi.lib().dp_sim_launch_count(self.handle)
 
     # -- fields -----------------------------------------------------------------
-    def _read(self, field: int, count: int) -> np.ndarray:
-        out = np.empty(count, dtype=np.float32)
+    def _read(self, field: int, count: int, out=None) -> np.ndarray:
+        out = _output(out, count)
         _abi.check(_abi.lib().dp_sim_read_field(self.handle, field, out.ctypes.data, count))
         return out
 
-    def read_electric(self) -> np.ndarray:
-        return self._read(_abi.DP_FIELD_ELECTRIC, 3 * self.cells)
+    def read_electric(self, out=None) -> np.ndarray:
+        return self._read(_abi.DP_FIELD_ELECTRIC, 3 * self.cells, out)
 
-    def read_magnetic(self) -> np.ndarray:
-        return self._read(_abi.DP_FIELD_MAGNETIC, 3 * self.cells)
+    def read_magnetic(self, out=None) -> np.ndarray:
+        return self._read(_abi.DP_FIELD_MAGNETIC, 3 * self.cells, out)
 
-    def read_intensity(self) -> np.ndarray:
-        return self._read(_abi.DP_FIELD_INTENSITY, self.cells)
+    def read_intensity(self, out=None) -> np.ndarray:
+        return self._read(_abi.DP_FIELD_INTENSITY, self.cells, out)
 
     def component(self, values: np.ndarray, axis: Axis) -> np.ndarray:
         a = int(axis)

@@ -38,3 +38,16 @@ def test_status_strings_and_errors():
     # A null scene is rejected with a status, not a crash.
     status = lib.dp_scene_create(None, None)
     assert status == 1 and b"null" in lib.dp_last_error()
+
+
+def test_read_buffers_are_checked_before_any_copy():
+    import numpy as np
+    import pytest
+    from diaphane_gb300.simulation import _output
+    assert _output(None, 5).shape == (5,)
+    buf = np.zeros((2, 4), dtype=np.float32)
+    view = _output(buf, 6)
+    assert view.shape == (6,) and np.shares_memory(view, buf)
+    for bad in [np.zeros(5, dtype=np.float64), np.zeros(4, dtype=np.float32), np.zeros((4, 4), np.float32)[:, 0]]:
+        with pytest.raises(ValueError):
+            _output(bad, 5)

@@ -99,3 +99,24 @@ def test_admission_refuses_what_the_arena_cannot_hold():
     with pytest.raises(DiaphaneError) as err:
         batch.add(r, 100)
     assert err.value.name == "DP_ERR_OOM"
+
+
+def test_reads_into_a_caller_buffer_match_fresh_arrays():
+    import torch
+    resolved = mixed(3, 30)
+    batch = Batch(ARENA, chunk_steps=16, max_scenes=4)
+    ids = [batch.add(r, 30, accumulate_intensity=True) for r in resolved]
+    batch.run_to_completion()
+    pinned = torch.empty(3 * max(r.cells for r in resolved) + 5, dtype=torch.float32, pin_memory=True).numpy()
+    for ident, r in zip(ids, resolved):
+        solo = Simulation(r)
+        solo.set_accumulate_intensity(True)
+        solo.advance_by(30)
+        for read_batch, read_solo in [(batch.read_electric, solo.read_electric),
+                                      (batch.read_magnetic, solo.read_magnetic),
+                                      (batch.read_intensity, solo.read_intensity)]:
+            fresh = read_batch(ident)
+            into = read_batch(ident, out=pinned)
+            assert into.size == fresh.size and np.shares_memory(into, pinned)
+            assert np.array_equal(bits(into), bits(fresh))
+            assert np.array_equal(bits(read_solo(out=pinned)), bits(fresh))
