@@ -762,8 +762,18 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
 // One scene: block b is tile b % tiles of z-chunk b / tiles.  Sixteen
 // resident warps x 128 registers fill each SM sub-partition's 16K-register
 // file exactly: two CTAs of 8 warps, or one of 16.
+// CTAs per SM a kernel variant is built for.  Narrow tiles give each warp
+// few cells per plane, so their fixed per-plane latency (ring waits,
+// barriers, the division chain) is hidden only by more resident warps: the
+// 64-wide form (3-slot ring, at most 80 registers) fits 3 CTAs per SM and the
+// 32-wide form (4-slot ring, 64 registers) 4, measured 14 % faster on a batch
+// of mixed small scenes than 2 CTAs of each.
+constexpr int resident_ctas(int CX, int TY, int SLOTS) {
+    return CX == 1 && SLOTS <= 4 ? 4 : (CX == 2 && SLOTS <= 3 ? 3 : 16 / TY);
+}
+
 template <int CX, int TY, int SLOTS>
-__global__ void __launch_bounds__(32 * TY, 16 / TY)
+__global__ void __launch_bounds__(32 * TY, resident_ctas(CX, TY, SLOTS))
 fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CUtensorMap h_map,
            const __grid_constant__ CUtensorMap m_map, const __grid_constant__ FusedArgs args) {
     const uint32_t tiles = args.tiles_x * args.tiles_y;
@@ -785,18 +795,8 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
 // A batch: block b is unit b of this variant's work list.  Scene descriptors
 // (with their tensor maps) live in global memory; a scene that has finished
 // its steps for this chunk, or has left the batch, is skipped.
-// CTAs per SM the batch kernel is built for.  Narrow tiles give each warp
-// few cells per plane, so their fixed per-plane latency (ring waits,
-// barriers, the division chain) is hidden only by more resident warps: the
-// 64-wide form (3-slot ring, 80 registers) fits 3 CTAs per SM and the 32-wide
-// form (4-slot ring, 64 registers) 4, measured 14 % faster on a batch of
-// mixed small scenes than 2 CTAs of each.
-constexpr int batch_blocks(int CX, int TY, int SLOTS) {
-    return CX == 1 && SLOTS <= 4 ? 4 : (CX == 2 && SLOTS <= 3 ? 3 : 16 / TY);
-}
-
 template <int CX, int TY, int SLOTS>
-__global__ void __launch_bounds__(32 * TY, batch_blocks(CX, TY, SLOTS))
+__global__ void __launch_bounds__(32 * TY, resident_ctas(CX, TY, SLOTS))
 fused_batch_step(const BatchScene *__restrict__ scenes, const BatchUnit *__restrict__ units,
                  const DeviceInjection *__restrict__ injections, const uint32_t *__restrict__ injection_counts,
                  uint32_t scene_count, uint32_t step, int32_t *error) {
@@ -871,9 +871,9 @@ template <int CX, int TY, int SLOTS> size_t smem_of() { return Geometry<CX, TY, 
 
 size_t variant_smem(uint32_t cx, uint32_t ty, uint32_t slots) {
     if (cx == 4 && ty == 8 && slots == 3) return smem_of<4, 8, 3>();
-    if (cx == 2 && ty == 8 && slots == 5) return smem_of<2, 8, 5>();
+    if (cx == 2 && ty == 8 && slots == 3) return smem_of<2, 8, 3>();
     if (cx == 4 && ty == 16 && slots == 3) return smem_of<4, 16, 3>();
-    if (cx == 1 && ty == 8 && slots == 5) return smem_of<1, 8, 5>();
+    if (cx == 1 && ty == 8 && slots == 4) return smem_of<1, 8, 4>();
     return 0;
 }
 
@@ -908,10 +908,10 @@ FusedPlan fused_plan(const uint32_t n[3], uint32_t cx, uint32_t tile_y, uint32_t
     FusedPlan p{};
     p.cx = cx ? cx : uint32_t(pick_cx(n[0]));
     p.tile_y = tile_y ? tile_y : 8;
-    p.slots = slots ? slots : (p.cx == 4 && p.tile_y == 8 ? 3 : (p.tile_y == 16 ? 3 : 5));
+    p.slots = slots ? slots : (p.cx == 1 && p.tile_y == 8 ? 4 : 3);
     p.smem = variant_smem(p.cx, p.tile_y, p.slots);
     if (p.smem == 0) throw std::runtime_error("no fused kernel variant with that tile shape and ring depth");
-    p.ctas_per_sm = 16 / p.tile_y;
+    p.ctas_per_sm = uint32_t(resident_ctas(int(p.cx), int(p.tile_y), int(p.slots)));
     const uint32_t tx = 32u * p.cx;
     p.tiles_x = (n[0] + tx - 1) / tx;
     p.tiles_y = (n[1] + p.tile_y - 1) / p.tile_y;
@@ -1036,9 +1036,10 @@ void launch_fused_step(const DeviceScene &s, const FusedPlan &plan, const FusedM
     args.z_chunk = plan.z_chunk;
     args.inj = table;
     if (plan.cx == 4 && plan.tile_y == 8 && plan.slots == 3) launch_variant<4, 8, 3>(plan, in_maps, args, stream);
-    else if (plan.cx == 2 && plan.tile_y == 8 && plan.slots == 5) launch_variant<2, 8, 5>(plan, in_maps, args, stream);
+    else if (plan.cx == 2 && plan.tile_y == 8 && plan.slots == 3) launch_variant<2, 8, 3>(plan, in_maps, args, stream);
     else if (plan.cx == 4 && plan.tile_y == 16 && plan.slots == 3) launch_variant<4, 16, 3>(plan, in_maps, args, stream);
-    else launch_variant<1, 8, 5>(plan, in_maps, args, stream);
+    else if (plan.cx == 1 && plan.tile_y == 8 && plan.slots == 4) launch_variant<1, 8, 4>(plan, in_maps, args, stream);
+    else throw std::runtime_error("no fused kernel variant with that tile shape and ring depth");
 }
 
 } // namespace diaphane
