@@ -872,8 +872,10 @@ template <int CX, int TY, int SLOTS> size_t smem_of() { return Geometry<CX, TY, 
 size_t variant_smem(uint32_t cx, uint32_t ty, uint32_t slots) {
     if (cx == 4 && ty == 8 && slots == 3) return smem_of<4, 8, 3>();
     if (cx == 2 && ty == 8 && slots == 3) return smem_of<2, 8, 3>();
+    if (cx == 2 && ty == 8 && slots == 5) return smem_of<2, 8, 5>();
     if (cx == 4 && ty == 16 && slots == 3) return smem_of<4, 16, 3>();
     if (cx == 1 && ty == 8 && slots == 4) return smem_of<1, 8, 4>();
+    if (cx == 1 && ty == 8 && slots == 5) return smem_of<1, 8, 5>();
     return 0;
 }
 
@@ -908,14 +910,29 @@ FusedPlan fused_plan(const uint32_t n[3], uint32_t cx, uint32_t tile_y, uint32_t
     FusedPlan p{};
     p.cx = cx ? cx : uint32_t(pick_cx(n[0]));
     p.tile_y = tile_y ? tile_y : 8;
-    p.slots = slots ? slots : (p.cx == 1 && p.tile_y == 8 ? 4 : 3);
-    p.smem = variant_smem(p.cx, p.tile_y, p.slots);
-    if (p.smem == 0) throw std::runtime_error("no fused kernel variant with that tile shape and ring depth");
-    p.ctas_per_sm = uint32_t(resident_ctas(int(p.cx), int(p.tile_y), int(p.slots)));
     const uint32_t tx = 32u * p.cx;
     p.tiles_x = (n[0] + tx - 1) / tx;
     p.tiles_y = (n[1] + p.tile_y - 1) / p.tile_y;
     const uint32_t tiles = p.tiles_x * p.tiles_y;
+    if (slots == 0) {
+        // The 64- and 32-wide tiles come in two builds: 3 or 4 CTAs per SM
+        // (shallow ring, fewer registers) for grids that fill the GPU, and 2
+        // CTAs per SM (5-slot ring, no register cap) for grids too small to
+        // give every SM that many CTAs even in 16-plane chunks, where each
+        // CTA's own latency is what counts.
+        p.slots = p.cx == 1 && p.tile_y == 8 ? 4 : 3;
+        if ((p.cx == 1 || p.cx == 2) && p.tile_y == 8) {
+            const uint64_t shallow = uint64_t(tiles) * ((n[2] + 15) / 16);
+            const uint64_t slots_on_gpu =
+                uint64_t(resident_ctas(int(p.cx), 8, int(p.slots))) * uint64_t(sm_count > 0 ? sm_count : 1);
+            if (shallow < slots_on_gpu) p.slots = 5;
+        }
+    } else {
+        p.slots = slots;
+    }
+    p.smem = variant_smem(p.cx, p.tile_y, p.slots);
+    if (p.smem == 0) throw std::runtime_error("no fused kernel variant with that tile shape and ring depth");
+    p.ctas_per_sm = uint32_t(resident_ctas(int(p.cx), int(p.tile_y), int(p.slots)));
     if (z_chunk == 0) {
         // Pick the chunk depth whose CTA count fills whole waves best, among
         // depths of at least 16 planes (each chunk rebuilds one extra plane).
@@ -1039,6 +1056,8 @@ void launch_fused_step(const DeviceScene &s, const FusedPlan &plan, const FusedM
     else if (plan.cx == 2 && plan.tile_y == 8 && plan.slots == 3) launch_variant<2, 8, 3>(plan, in_maps, args, stream);
     else if (plan.cx == 4 && plan.tile_y == 16 && plan.slots == 3) launch_variant<4, 16, 3>(plan, in_maps, args, stream);
     else if (plan.cx == 1 && plan.tile_y == 8 && plan.slots == 4) launch_variant<1, 8, 4>(plan, in_maps, args, stream);
+    else if (plan.cx == 2 && plan.tile_y == 8 && plan.slots == 5) launch_variant<2, 8, 5>(plan, in_maps, args, stream);
+    else if (plan.cx == 1 && plan.tile_y == 8 && plan.slots == 5) launch_variant<1, 8, 5>(plan, in_maps, args, stream);
     else throw std::runtime_error("no fused kernel variant with that tile shape and ring depth");
 }
 

@@ -80,7 +80,7 @@ extern "C" dp_status dp_sim_autotune(dp_sim *sim, uint32_t steps, dp_tuning *out
         check_cuda(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sim->device), "attribute");
         const uint32_t *n = sim->scene.grid.n;
         std::vector<Candidate> candidates;
-        const Candidate shapes[] = {{4, 8, 3, 0}, {2, 8, 3, 0}, {4, 16, 3, 0}, {1, 8, 4, 0}};
+        const Candidate shapes[] = {{4, 8, 3, 0}, {2, 8, 3, 0}, {2, 8, 5, 0}, {4, 16, 3, 0}, {1, 8, 4, 0}, {1, 8, 5, 0}};
         for (const Candidate &shape : shapes) {
             if (!fused_variant_exists(shape.cx, shape.ty, shape.slots)) continue;
             // The wave-filling depth the planner picks (0), and fixed depths.

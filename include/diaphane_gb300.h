@@ -325,7 +325,8 @@ typedef struct dp_batch_options {
     uint32_t max_scenes;  /* scene slots; 0 = 256 */
     uint32_t use_graphs;  /* 0: launch each chunk's kernels directly */
     uint32_t cells_per_lane; /* tile width 32·this for every scene (1, 2 or 4); 0 = per scene, least waste */
-    uint32_t unit_planes;    /* z-planes per work unit; 0 = 24 */
+    uint32_t unit_planes;    /* z-planes per work unit; 0 = chosen when the work list is rebuilt:
+                                64 when the batch holds 16 units per SM at that depth, else 24 */
 } dp_batch_options;
 
 dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out);

@@ -142,7 +142,7 @@ def test_heterogeneous_workload_at_small_size_matches(threads):
     assert np.array_equal(reference.read_intensity().view(np.uint32), candidate.read_intensity().view(np.uint32))
 
 
-@pytest.mark.parametrize("variant", [(4, 8, 3), (2, 8, 3), (4, 16, 3), (1, 8, 4)])
+@pytest.mark.parametrize("variant", [(4, 8, 3), (2, 8, 3), (2, 8, 5), (4, 16, 3), (1, 8, 4), (1, 8, 5)])
 @pytest.mark.parametrize("case", ["materials", "plane_wave", "several_sources"])
 def test_every_fused_variant_is_bit_identical(variant, case, threads):
     """Tile width, tile height and ring depth are performance knobs only."""
