@@ -19,7 +19,7 @@ DP_ERR_OOM, DP_ERR_UNSUPPORTED, DP_ERR_RANGE, DP_ERR_BUSY = 5, 6, 7, 8
 DP_BOUNDARY_PEC, DP_BOUNDARY_ABSORBING = 0, 1
 DP_SHAPE_BLOCK, DP_SHAPE_SPHERE, DP_SHAPE_SLAB = 0, 1, 2
 DP_WAVE_RICKER, DP_WAVE_GAUSSIAN_PULSE, DP_WAVE_CONTINUOUS = 0, 1, 2
-DP_SOURCE_POINT, DP_SOURCE_SHEET, DP_SOURCE_PLANE_WAVE = 0, 1, 2
+DP_SOURCE_POINT, DP_SOURCE_SHEET, DP_SOURCE_PLANE_WAVE, DP_SOURCE_PLANE_WAVE_BOX = 0, 1, 2, 3
 DP_TABLE_MAGNETIC_GAINS, DP_TABLE_ELECTRIC_GAINS, DP_TABLE_CELL_CENTERS, DP_TABLE_ABSORBER = 0, 1, 2, 3
 DP_TABLE_COEFFICIENTS, DP_TABLE_MATERIAL_INDEX, DP_TABLE_PRIMARY, DP_TABLE_DUAL = 4, 5, 6, 7
 DP_MAP_TO_CELL, DP_MAP_TO_POSITION, DP_MAP_CELL_CONTAINING, DP_MAP_CELL_CENTER = 0, 1, 2, 3
@@ -61,7 +61,7 @@ class dp_waveform(C.Structure):
 class dp_source(C.Structure):
     _fields_ = [("shape", C.c_uint32), ("polarization", C.c_uint32), ("at", F3), ("velocity", F3),
                 ("axis", C.c_uint32), ("offset", C.c_float), ("waist", C.c_float), ("amplitude", C.c_float),
-                ("waveform", dp_waveform)]
+                ("waveform", dp_waveform), ("box_low", F3), ("box_high", F3)]
 
 
 class dp_scene_desc(C.Structure):

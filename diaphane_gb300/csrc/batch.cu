@@ -379,6 +379,8 @@ struct dp_batch {
                     d.magnetic = si.magnetic;
                     d.value = si.value;
                     d.weight_offset = si.weight_offset;
+                    d.profile_offset = -1; // a batch scene has no total-field box
+                    d.profile_axis = 0;
                 }
                 hc[size_t(t) * capacity + e.slot] = n;
             }
@@ -544,6 +546,9 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         if (2 * s.sources.size() > size_t(kBatchInjections))
             throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 4 sources");
         if (s.index_bytes != 1) throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 256 materials");
+        if (s.has_boxes())
+            throw Error(DP_ERR_UNSUPPORTED, "a batch scene takes no total-field box (its side faces need per-step "
+                                            "profiles the batch does not stage)");
         uint32_t slot = 0;
         while (slot < b->capacity && b->slot_used[slot]) ++slot;
         if (slot == b->capacity) throw Error(DP_ERR_BUSY, "every scene slot of the batch is in use");

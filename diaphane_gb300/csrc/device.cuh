@@ -39,14 +39,31 @@ struct DeviceInjection {
     uint32_t magnetic;
     float value;
     int32_t weight_offset; // -1: weight 1
+    // A total-field box's side face: the cell's weight is the step's
+    // profile value at profile_offset + (coordinate - origin) along
+    // profile_axis; -1: none.
+    int32_t profile_offset;
+    uint32_t profile_axis;
 };
 
 // Non-silent injections of one step, in the reference's application order.
 constexpr int kMaxInjections = 32;
 struct InjectionTable {
     uint32_t count;
+    const float *profiles; // the step's box profile values (device), or null
     DeviceInjection item[kMaxInjections];
 };
+
+// The weight of cell (x, y, z) of injection d (d's box contains the cell).
+template <typename T>
+__device__ __forceinline__ T injection_weight(const DeviceInjection &d, const float *weights, const T *profiles,
+                                              uint32_t x, uint32_t y, uint32_t z, uint64_t index_in_box) {
+    if (d.profile_offset >= 0 && profiles != nullptr) {
+        const uint32_t c = d.profile_axis == 0 ? x : (d.profile_axis == 1 ? y : z);
+        return profiles[d.profile_offset + int32_t(c - d.origin[d.profile_axis])];
+    }
+    return d.weight_offset < 0 ? T(1) : T(__ldg(&weights[d.weight_offset + index_in_box]));
+}
 
 // Fields of one buffer set: component a of E at e + a*cells.  The step runs
 // in float; the FP64 instance keeps its fields in double.
@@ -63,9 +80,12 @@ void launch_naive_magnetic(const DeviceScene &s, FieldSet f, bool reverse, cudaS
 void launch_naive_magnetic(const DeviceScene &s, FieldSet64 f, bool reverse, cudaStream_t stream);
 void launch_naive_electric(const DeviceScene &s, FieldSet f, bool reverse, cudaStream_t stream);
 void launch_naive_electric(const DeviceScene &s, FieldSet64 f, bool reverse, cudaStream_t stream);
-void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj, float sign, cudaStream_t stream);
+// `profiles`: the step's box profile values (device) when inj has one.
+void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj, float sign, const float *profiles,
+                   cudaStream_t stream);
 // `value` is the signed drive in double; inj.value is not read.
-void launch_inject(const DeviceScene &s, FieldSet64 f, const DeviceInjection &inj, double value, cudaStream_t stream);
+void launch_inject(const DeviceScene &s, FieldSet64 f, const DeviceInjection &inj, double value,
+                   const double *profiles, cudaStream_t stream);
 void launch_intensity(const DeviceScene &s, const float *e, float *intensity, cudaStream_t stream);
 
 // Dense <-> pitched rows of `components` fields of `rows` rows each (pitch.cu).

@@ -268,6 +268,7 @@ __device__ __forceinline__ void divide_compacted(float *scratch, int items_max, 
 struct InjectionView {
     const DeviceInjection *item;
     uint32_t count;
+    const float *profiles; // total-field box profile values of the step, or null
 };
 
 __device__ __forceinline__ uint32_t injection_mask(const InjectionView &t, bool magnetic, int xa, int xb, int y) {
@@ -297,9 +298,8 @@ __device__ __forceinline__ void apply_injections(const InjectionView &t, const f
         for (int j = 0; j < CX; ++j) {
             const int dx = x + j - int(d.origin[0]);
             if (dx < 0 || dx >= int(d.extent[0])) continue;
-            const float w = d.weight_offset < 0
-                                ? 1.0f
-                                : __ldg(&weights[d.weight_offset + (uint64_t(dz) * d.extent[1] + dy) * d.extent[0] + dx]);
+            const float w = injection_weight<float>(d, weights, t.profiles, uint32_t(x + j), uint32_t(y), uint32_t(z),
+                                                    (uint64_t(dz) * d.extent[1] + dy) * d.extent[0] + dx);
             const float add = d.value * w;
             if (d.component == 0) f0.v[j] += add;
             else if (d.component == 1) f1.v[j] += add;
@@ -784,7 +784,7 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
     u.h_out = args.h_out;
     u.intensity = args.intensity;
     u.error = args.error;
-    u.inj = InjectionView{args.inj.item, args.inj.count};
+    u.inj = InjectionView{args.inj.item, args.inj.count, args.inj.profiles};
     u.x0 = int(tile % args.tiles_x) * 32 * CX;
     u.y0 = int(tile / args.tiles_x) * TY;
     u.z0 = int(chunk * args.z_chunk);
@@ -820,7 +820,7 @@ fused_batch_step(const BatchScene *__restrict__ scenes, const BatchUnit *__restr
     u.intensity = bs.intensity;
     u.error = error;
     const size_t slot = size_t(step) * scene_count + unit.scene;
-    u.inj = InjectionView{injections + slot * kBatchInjections, injection_counts[slot]};
+    u.inj = InjectionView{injections + slot * kBatchInjections, injection_counts[slot], nullptr};
     u.x0 = int(unit.x0);
     u.y0 = int(unit.y0);
     u.z0 = int(unit.z0);

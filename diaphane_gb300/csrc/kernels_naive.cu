@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(kThreads) electric_pass(DeviceScene s, const T
 // One soft injection over its box (fdtd.wgsl inject, src/cpu.rs:618-629);
 // `value` is the drive with its sign applied.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) inject_pass(DeviceScene s, Fields<T> f, DeviceInjection inj, T value) {
+__global__ void __launch_bounds__(kThreads) inject_pass(DeviceScene s, Fields<T> f, DeviceInjection inj, T value,
+                                                        const T *__restrict__ profiles) {
     const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
     const uint64_t count = uint64_t(inj.extent[0]) * inj.extent[1] * inj.extent[2];
     if (i >= count) return;
@@ -114,9 +115,10 @@ __global__ void __launch_bounds__(kThreads) inject_pass(DeviceScene s, Fields<T>
     const uint32_t dy = uint32_t(t % inj.extent[1]);
     const uint32_t dz = uint32_t(t / inj.extent[1]);
     const uint64_t cell = (uint64_t(inj.origin[2] + dz) * s.n[1] + (inj.origin[1] + dy)) * s.pitch + inj.origin[0] + dx;
-    const float weight = inj.weight_offset < 0 ? 1.0f : __ldg(&s.weights[inj.weight_offset + i]);
+    const T weight = injection_weight<T>(inj, s.weights, profiles, inj.origin[0] + dx, inj.origin[1] + dy,
+                                         inj.origin[2] + dz, i);
     T *field = (inj.magnetic ? f.h : f.e) + uint64_t(inj.component) * s.cells;
-    field[cell] += value * T(weight);
+    field[cell] += value * weight;
 }
 
 // I += Ex² + Ey² + Ez² (src/cpu.rs:186-196).
@@ -220,10 +222,10 @@ template <typename T> void electric(const DeviceScene &s, Fields<T> f, bool reve
 }
 
 template <typename T> void inject(const DeviceScene &s, Fields<T> f, const DeviceInjection &inj, T value,
-                                  cudaStream_t stream) {
+                                  const T *profiles, cudaStream_t stream) {
     const uint64_t count = uint64_t(inj.extent[0]) * inj.extent[1] * inj.extent[2];
     if (count == 0) return;
-    inject_pass<T><<<blocks_for(count), kThreads, 0, stream>>>(s, f, inj, value);
+    inject_pass<T><<<blocks_for(count), kThreads, 0, stream>>>(s, f, inj, value, profiles);
 }
 
 } // namespace
@@ -242,11 +244,13 @@ void launch_naive_electric(const DeviceScene &s, FieldSet64 f, bool reverse, cud
 }
 
 // sign · value is exact (sign is ±1), so the f32 drive is the reference's.
-void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj, float sign, cudaStream_t stream) {
-    inject(s, f, inj, sign * inj.value, stream);
+void launch_inject(const DeviceScene &s, FieldSet f, const DeviceInjection &inj, float sign, const float *profiles,
+                   cudaStream_t stream) {
+    inject(s, f, inj, sign * inj.value, profiles, stream);
 }
-void launch_inject(const DeviceScene &s, FieldSet64 f, const DeviceInjection &inj, double value, cudaStream_t stream) {
-    inject(s, f, inj, value, stream);
+void launch_inject(const DeviceScene &s, FieldSet64 f, const DeviceInjection &inj, double value,
+                   const double *profiles, cudaStream_t stream) {
+    inject(s, f, inj, value, profiles, stream);
 }
 
 void launch_intensity(const DeviceScene &s, const float *e, float *intensity, cudaStream_t stream) {

@@ -411,7 +411,15 @@ Scene Scene::build(const dp_scene_desc &d) {
         if (sh.material >= d.material_count) invalid("a shape refers to a material outside the table");
     for (const auto &src : s.sources) {
         if (src.polarization > 2 || src.axis > 2) invalid("an axis index must be 0, 1 or 2");
-        if (src.shape > DP_SOURCE_PLANE_WAVE || src.waveform.kind > DP_WAVE_CONTINUOUS) invalid("unknown source or waveform kind");
+        if (src.shape > DP_SOURCE_PLANE_WAVE_BOX || src.waveform.kind > DP_WAVE_CONTINUOUS) invalid("unknown source or waveform kind");
+        if (src.shape == DP_SOURCE_PLANE_WAVE_BOX) {
+            if (src.polarization == src.axis) invalid("a plane wave's polarization must be transverse to its travel");
+            uint32_t lo[3], hi[3];
+            s.box_bounds(src, lo, hi);
+            for (int a = 0; a < 3; ++a)
+                if (!(lo[a] >= 1 && lo[a] < hi[a] && hi[a] + 2 <= s.grid.n[a]))
+                    invalid("a total-field box needs a cell of scattered field and a wall cell beyond each face");
+        }
     }
 
     const ResolvedGrid &g = s.grid;
@@ -466,11 +474,15 @@ Scene Scene::build(const dp_scene_desc &d) {
     // src/source.rs:441-455), evaluated once per sheet.
     s.source_weight.assign(s.sources.size(), -1);
     std::vector<StepInjection> probe;
-    for (size_t k = 0; k < s.sources.size(); ++k) {
+    std::vector<BoxCorrections<float>> no_boxes(s.sources.size()); // boxes add no slots here
+    std::vector<float> no_profiles;
+    for (size_t k = 0, slot = 0; k < s.sources.size(); ++k) {
         const dp_source &src = s.sources[k];
+        const size_t first = slot;
+        slot += src.shape == DP_SOURCE_PLANE_WAVE_BOX ? 0 : 2;
         if (src.shape != DP_SOURCE_SHEET) continue;
-        s.injections(0.0f, probe); // the box does not depend on time
-        const StepInjection &inj = probe[2 * k];
+        s.injections_in<float>(0.0f, probe, &no_boxes, &no_profiles); // the sheet's box does not depend on time
+        const StepInjection &inj = probe[first];
         s.source_weight[k] = int32_t(s.weights.size());
         for (uint32_t dz = 0; dz < inj.extent[2]; ++dz)
             for (uint32_t dy = 0; dy < inj.extent[1]; ++dy)
@@ -484,12 +496,44 @@ Scene Scene::build(const dp_scene_desc &d) {
     return s;
 }
 
+size_t Scene::injection_slots() const {
+    size_t n = 0;
+    for (const dp_source &src : sources) n += src.shape == DP_SOURCE_PLANE_WAVE_BOX ? 8 : 2;
+    return n;
+}
+
+bool Scene::has_boxes() const {
+    for (const dp_source &src : sources)
+        if (src.shape == DP_SOURCE_PLANE_WAVE_BOX) return true;
+    return false;
+}
+
+void Scene::box_bounds(const dp_source &src, uint32_t lo[3], uint32_t hi[3]) const {
+    grid.cell_containing(src.box_low, lo);
+    grid.cell_containing(src.box_high, hi);
+}
+
 // Source::injections, src/source.rs:280-403: two slots per source.
-template <typename T> void Scene::injections_in(T time, std::vector<InjectionOf<T>> &out) const {
+template <typename T>
+void Scene::injections_in(T time, std::vector<InjectionOf<T>> &out, const std::vector<BoxCorrections<T>> *boxes,
+                          std::vector<T> *profiles) const {
     out.clear();
+    if (profiles) profiles->clear();
     const ResolvedGrid &g = grid;
     for (size_t k = 0; k < sources.size(); ++k) {
         const dp_source &src = sources[k];
+        if (src.shape == DP_SOURCE_PLANE_WAVE_BOX) {
+            if (!boxes || !profiles)
+                throw Error(DP_ERR_UNSUPPORTED, "a total-field box's corrections depend on its incident line's history");
+            const BoxCorrections<T> &b = (*boxes)[k];
+            const int32_t base = int32_t(profiles->size());
+            for (InjectionOf<T> inj : b.items) {
+                if (inj.profile_offset >= 0) inj.profile_offset += base;
+                out.push_back(inj);
+            }
+            profiles->insert(profiles->end(), b.profiles.begin(), b.profiles.end());
+            continue;
+        }
         const T value = T(src.amplitude) * waveform_in<T>(src.waveform, time);
         InjectionOf<T> a{}, b{};
         a.weight_offset = b.weight_offset = -1;
@@ -554,7 +598,236 @@ template <typename T> void Scene::injections_in(T time, std::vector<InjectionOf<
     }
 }
 
-template void Scene::injections_in<float>(float, std::vector<InjectionOf<float>> &) const;
-template void Scene::injections_in<double>(double, std::vector<InjectionOf<double>> &) const;
+template void Scene::injections_in<float>(float, std::vector<InjectionOf<float>> &,
+                                         const std::vector<BoxCorrections<float>> *, std::vector<float> *) const;
+template void Scene::injections_in<double>(double, std::vector<InjectionOf<double>> &,
+                                          const std::vector<BoxCorrections<double>> *, std::vector<double> *) const;
+
+// ---------------------------------------------------------------------------
+// Total-field boxes: the incident lines and the face corrections.
+//
+// Every E and H node of the Yee cell is inside the total field when its
+// position lies within the box [lo, hi] (cell units, E-node indices): along
+// its own axis an E node sits half a cell up and an H node on the index, so
+// E_q is inside for lo_q <= i_q <= hi_q - 1 and H_q for lo_q <= i_q <= hi_q,
+// and the other way round across.  An update that reads a node on the other
+// side of the surface reads the wrong field there; it is corrected by the
+// update's coefficient times the incident value at that node: added for a
+// total node reading a scattered one, subtracted the other way.  With the
+// incident E along p and H along h (a the travel axis) that leaves E_p and H_h
+// on the two faces across a (uniform over the face), and the travel
+// components on the side faces: H_a on the faces across h, E_a on the faces
+// across p, whose incident values vary along a.  For the face across a at
+// the entry this is exactly the reference's plane wave (src/source.rs:334-401).
+// ---------------------------------------------------------------------------
+
+namespace {
+constexpr int kLineMargin = 8;  // line cells before the box and after it
+constexpr int kLineTail = 64;   // absorbing cells at the line's far end
+constexpr uint64_t kLineCheckpoint = 256;
+float sign_if(bool b) { return b ? 1.0f : -1.0f; }
+} // namespace
+
+template <typename T> IncidentLines<T>::IncidentLines(const Scene &scene) {
+    const ResolvedGrid &g = scene.grid;
+    sources_ = scene.sources.size();
+    dt_ = scene.dt;
+    for (size_t k = 0; k < scene.sources.size(); ++k) {
+        const dp_source &src = scene.sources[k];
+        if (src.shape != DP_SOURCE_PLANE_WAVE_BOX) continue;
+        Line l{};
+        l.source = k;
+        l.src = src;
+        l.a = int(src.axis);
+        l.p = int(src.polarization);
+        l.h = 3 - l.a - l.p;
+        uint32_t lo[3], hi[3];
+        scene.box_bounds(src, lo, hi);
+        for (int i = 0; i < 3; ++i) {
+            l.lo[i] = int(lo[i]);
+            l.hi[i] = int(hi[i]);
+        }
+        const int a = l.a, n_a = int(g.n[a]);
+        l.first = l.lo[a] - kLineMargin;
+        l.inject = kLineMargin / 2; // the line's own E row, lo_a - 4
+        const int last = l.hi[a] + kLineMargin + kLineTail;
+        const size_t count = size_t(last - l.first + 1);
+        l.e.assign(count, T(0));
+        l.hf.assign(count, T(0));
+        l.ge.resize(count);
+        l.gm.resize(count);
+        l.le.assign(count, 0.0f);
+        l.lm.assign(count, 0.0f);
+        const uint32_t off_a = scene.axis_offset(a);
+        for (size_t i = 0; i < count; ++i) {
+            const int c = std::min(std::max(l.first + int(i), 0), n_a - 1);
+            l.ge[i] = scene.electric_gains[off_a + uint32_t(c)];
+            l.gm[i] = scene.magnetic_gains[off_a + uint32_t(c)];
+        }
+        // The tail: the absorbing profile's polynomial grading (the same form
+        // as the grid's, src/boundary.rs:100-196) over the last cells.
+        const float t = float(kLineTail);
+        const float peak = -(3.0f + 1.0f) * std::log(1e-6f) * g.courant / (4.0f * t);
+        const int tail0 = int(count) - kLineTail;
+        for (int i = tail0; i < int(count); ++i) {
+            const float de = std::fmin(float(i - tail0 + 1) / t, 1.0f);
+            const float dh = std::fmin((float(i - tail0) + 1.5f) / t, 1.0f);
+            l.le[size_t(i)] = peak * de * de * de;
+            l.lm[size_t(i)] = peak * dh * dh * dh;
+        }
+        // The plane-wave drive of src/source.rs:334-401, for the line's row.
+        const float spacing = g.axes[a].finest();
+        const T dt = T(g.time_step());
+        l.gain = T(kSpeedOfLight * g.time_step() / spacing);
+        const T omega = T(2) * pi_in<T>() * T(src.waveform.frequency);
+        const T half_k_spacing = std::asin(std::sin(T(0.5) * omega * dt) / l.gain);
+        l.retard = half_k_spacing / omega;
+        l.h_sign = ((l.p + 1) % 3) == a ? T(-1) : T(1);
+        // Curl signs: E_p += sigma_e g (H_h[i] - H_h[i-1]); H_h -= sigma_h g
+        // (E_p[i+1] - E_p[i]); H_a's term in E_p across h and E_a's in H_h
+        // across p carry sigma_ha and sigma_ea.
+        l.sigma_e = sign_if((l.p + 1) % 3 == a);
+        l.sigma_h = sign_if((l.h + 1) % 3 == a);
+        l.sigma_ha = sign_if((a + 2) % 3 == l.p);
+        l.sigma_ea = sign_if((a + 2) % 3 == l.h);
+        const uint32_t off_p = scene.axis_offset(l.p), off_h = scene.axis_offset(l.h);
+        l.face_e[0] = scene.electric_gains[off_a + uint32_t(l.lo[a])];
+        l.face_e[1] = scene.electric_gains[off_a + uint32_t(l.hi[a])];
+        l.face_h[0] = scene.magnetic_gains[off_a + uint32_t(l.lo[a] - 1)];
+        l.face_h[1] = scene.magnetic_gains[off_a + uint32_t(l.hi[a])];
+        l.side_h[0] = scene.magnetic_gains[off_h + uint32_t(l.lo[l.h] - 1)];
+        l.side_h[1] = scene.magnetic_gains[off_h + uint32_t(l.hi[l.h])];
+        l.side_e[0] = scene.electric_gains[off_p + uint32_t(l.lo[l.p])];
+        l.side_e[1] = scene.electric_gains[off_p + uint32_t(l.hi[l.p])];
+        const int span = l.hi[a] - l.lo[a];
+        profile_width_ += size_t(2 * (span + 1) + 2 * span);
+        lines_.push_back(std::move(l));
+    }
+    std::vector<std::vector<T>> start;
+    for (const Line &l : lines_) {
+        start.push_back(l.e);
+        start.push_back(l.hf);
+    }
+    checkpoints_.emplace_back(0, std::move(start));
+}
+
+template <typename T> const std::vector<BoxCorrections<T>> &IncidentLines<T>::at(uint64_t step) {
+    if (cached_ == step) return cache_;
+    if (state_ > step) {
+        size_t c = checkpoints_.size() - 1;
+        while (checkpoints_[c].first > step) --c;
+        for (size_t i = 0; i < lines_.size(); ++i) {
+            lines_[i].e = checkpoints_[c].second[2 * i];
+            lines_[i].hf = checkpoints_[c].second[2 * i + 1];
+        }
+        state_ = checkpoints_[c].first;
+    }
+    while (state_ < step) advance(state_, nullptr);
+    cache_.assign(sources_, BoxCorrections<T>{});
+    advance(state_, &cache_);
+    cached_ = step;
+    return cache_;
+}
+
+// One step of every line (H, its drive, E, its drive), recording the box
+// corrections of that step first when `out` is given.
+template <typename T> void IncidentLines<T>::advance(uint64_t step, std::vector<BoxCorrections<T>> *out) {
+    const T time = step_time<T>(step, dt_);
+    const T dt = std::is_same_v<T, float> ? T(dt_) : T(double(dt_));
+    for (Line &l : lines_) {
+        const int a = l.a, p = l.p, h = l.h;
+        const size_t count = l.e.size();
+        auto E = [&](int cell) { return l.e[size_t(cell - l.first)]; };
+        auto H = [&](int cell) { return l.hf[size_t(cell - l.first)]; };
+        auto slot = [&](int component, bool magnetic) {
+            InjectionOf<T> inj{};
+            inj.component = uint32_t(component);
+            inj.magnetic = magnetic ? 1u : 0u;
+            inj.weight_offset = -1;
+            inj.origin[a] = uint32_t(l.lo[a]);
+            inj.extent[a] = uint32_t(l.hi[a] - l.lo[a]);
+            inj.origin[p] = uint32_t(l.lo[p]);
+            inj.extent[p] = uint32_t(l.hi[p] - l.lo[p]);
+            inj.origin[h] = uint32_t(l.lo[h]);
+            inj.extent[h] = uint32_t(l.hi[h] - l.lo[h] + 1);
+            return inj;
+        };
+        BoxCorrections<T> *box = out ? &(*out)[l.source] : nullptr;
+        std::vector<InjectionOf<T>> magnetic;
+        if (box) {
+            // H phase: the incident E at step·dt.
+            for (int f = 0; f < 2; ++f) {
+                InjectionOf<T> inj = slot(h, true);
+                inj.origin[a] = uint32_t(f ? l.hi[a] : l.lo[a] - 1);
+                inj.extent[a] = 1;
+                inj.value = T(l.sigma_h * (f ? -l.face_h[1] : l.face_h[0])) * E(f ? l.hi[a] : l.lo[a]);
+                magnetic.push_back(inj);
+            }
+            for (int f = 0; f < 2; ++f) {
+                InjectionOf<T> inj = slot(a, true);
+                inj.extent[a] = uint32_t(l.hi[a] - l.lo[a] + 1);
+                inj.origin[h] = uint32_t(f ? l.hi[h] : l.lo[h] - 1);
+                inj.extent[h] = 1;
+                inj.value = T(1);
+                inj.profile_offset = int32_t(box->profiles.size());
+                inj.profile_axis = uint32_t(a);
+                const T coef = T(l.sigma_ha * (f ? -l.side_h[1] : l.side_h[0]));
+                for (int c = l.lo[a]; c <= l.hi[a]; ++c) box->profiles.push_back(coef * E(c));
+                magnetic.push_back(inj);
+            }
+        }
+        // H of the line: the same update the grid makes on a wave uniform
+        // across it, and the absorbing tail.
+        for (size_t i = 0; i < count; ++i) {
+            const T next = i + 1 < count ? l.e[i + 1] : T(0);
+            const T curl = T(l.sigma_h) * (T(l.gm[i]) * (next - l.e[i]));
+            const T loss = T(l.lm[i]);
+            l.hf[i] = loss == T(0) ? l.hf[i] - curl : ((T(1) - loss) * l.hf[i] - curl) / (T(1) + loss);
+        }
+        const T amplitude = T(l.src.amplitude);
+        l.hf[size_t(l.inject - 1)] += l.h_sign * l.gain * (amplitude * waveform_in<T>(l.src.waveform, time - dt));
+        if (box) {
+            // E phase: the incident H at (step + 1/2)·dt.
+            for (int f = 0; f < 2; ++f) {
+                InjectionOf<T> inj = slot(p, false);
+                inj.origin[a] = uint32_t(f ? l.hi[a] : l.lo[a]);
+                inj.extent[a] = 1;
+                inj.value = T(l.sigma_e * (f ? l.face_e[1] : -l.face_e[0])) * H(f ? l.hi[a] : l.lo[a] - 1);
+                box->items.push_back(inj);
+            }
+            for (int f = 0; f < 2; ++f) {
+                InjectionOf<T> inj = slot(a, false);
+                inj.origin[p] = uint32_t(f ? l.hi[p] : l.lo[p]);
+                inj.extent[p] = 1;
+                inj.value = T(1);
+                inj.profile_offset = int32_t(box->profiles.size());
+                inj.profile_axis = uint32_t(a);
+                const T coef = T(l.sigma_ea * (f ? l.side_e[1] : -l.side_e[0]));
+                for (int c = l.lo[a]; c < l.hi[a]; ++c) box->profiles.push_back(coef * H(c));
+                box->items.push_back(inj);
+            }
+            box->items.insert(box->items.end(), magnetic.begin(), magnetic.end());
+        }
+        for (size_t i = 1; i < count; ++i) {
+            const T curl = T(l.sigma_e) * (T(l.ge[i]) * (l.hf[i] - l.hf[i - 1]));
+            const T loss = T(l.le[i]);
+            l.e[i] = loss == T(0) ? l.e[i] + curl : ((T(1) - loss) * l.e[i] + curl) / (T(1) + loss);
+        }
+        l.e[size_t(l.inject)] +=
+            l.gain * (amplitude * waveform_in<T>(l.src.waveform, time - T(0.5) * dt + l.retard));
+    }
+    ++state_;
+    if (state_ % kLineCheckpoint == 0 && checkpoints_.back().first < state_) {
+        std::vector<std::vector<T>> snap;
+        for (const Line &l : lines_) {
+            snap.push_back(l.e);
+            snap.push_back(l.hf);
+        }
+        checkpoints_.emplace_back(state_, std::move(snap));
+    }
+}
+
+template class IncidentLines<float>;
+template class IncidentLines<double>;
 
 } // namespace diaphane

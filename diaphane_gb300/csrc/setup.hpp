@@ -10,6 +10,7 @@
 #include <cstdint>
 #include <stdexcept>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 namespace diaphane {
@@ -79,8 +80,27 @@ template <typename T> struct InjectionOf {
     int32_t weight_offset; // into Scene::weights, -1 when every cell weighs 1
     float inverse_waist_squared;
     float center[3];
+    // A total-field box's side-face correction varies along the travel axis:
+    // a cell then adds value (1) times profile[profile_offset + coord -
+    // origin] along profile_axis, from the step's profile values; -1: none.
+    int32_t profile_offset = -1;
+    uint32_t profile_axis = 0;
 };
 using StepInjection = InjectionOf<float>;
+
+// The time of step `step`'s injections, (step + 1)·dt, as the step computes
+// it: an f32 product for the f32 step, exact in f64 for the FP64 instance.
+template <typename T> T step_time(uint64_t step, float dt) {
+    if constexpr (std::is_same_v<T, float>) return float(step + 1) * dt;
+    else return T(step + 1) * T(dt);
+}
+
+// The eight corrections of one total-field box for one step, in application
+// order (four on E, then four on H), and the side faces' per-cell values.
+template <typename T> struct BoxCorrections {
+    std::vector<InjectionOf<T>> items;
+    std::vector<T> profiles;
+};
 
 // The resolved scene: the tables the kernels read.
 struct Scene {
@@ -129,10 +149,66 @@ struct Scene {
     uint32_t lookup_samples() const;
     uint32_t axis_offset(int axis) const { return axis == 0 ? 0 : (axis == 1 ? grid.n[0] : grid.n[0] + grid.n[1]); }
 
-    // Source::injections for every source at `time`, two slots per source.
+    // Source::injections for every source at `time`, two slots per source
+    // (a total-field box, whose corrections depend on the history of its
+    // incident line, is refused here).
     void injections(float time, std::vector<StepInjection> &out) const { injections_in<float>(time, out); }
     // The same with time and drive in T (float and double are instantiated).
-    template <typename T> void injections_in(T time, std::vector<InjectionOf<T>> &out) const;
+    // `boxes`, indexed by source, supplies the total-field boxes' corrections
+    // of this step; their profile offsets are rebased onto `profiles`.
+    template <typename T>
+    void injections_in(T time, std::vector<InjectionOf<T>> &out, const std::vector<BoxCorrections<T>> *boxes = nullptr,
+                       std::vector<T> *profiles = nullptr) const;
+    // Injection slots per step: 8 for a total-field box, 2 for any other source.
+    size_t injection_slots() const;
+    bool has_boxes() const;
+    // A box source's total field in cells: E-node index bounds per axis.
+    void box_bounds(const dp_source &src, uint32_t lo[3], uint32_t hi[3]) const;
+};
+
+// The incident field of every total-field box of a scene: a 1-D Yee line
+// along the box's travel axis, stepped with the grid's own gains there so the
+// box faces cancel what the 3-D stencil propagates (dispersion included),
+// driven by the one-way plane-wave corrections of src/source.rs:334-401 a few
+// cells before the box, and ending in a graded absorbing tail.  The lines'
+// state is a function of the step count alone: a request for an earlier step
+// replays from the last checkpoint (every 256 steps) before it.
+template <typename T> class IncidentLines {
+  public:
+    IncidentLines() = default;
+    explicit IncidentLines(const Scene &scene);
+    bool empty() const { return lines_.empty(); }
+    // Per source (empty for sources that are not boxes): the corrections of
+    // step `step`.  Computed once per step; the lines then stand at step + 1.
+    const std::vector<BoxCorrections<T>> &at(uint64_t step);
+    // Values of the step's profiles in total, over all boxes.
+    size_t profile_width() const { return profile_width_; }
+
+  private:
+    struct Line {
+        size_t source;
+        int a, p, h;                // travel, polarization and incident-H axes
+        int lo[3], hi[3];           // the box
+        int first;                  // cell index (along a) of element 0
+        int inject;                 // element of the line's own plane-wave E row
+        std::vector<T> e, hf;       // E at element i, H half an element on
+        std::vector<float> ge, gm;  // the grid's gains at those cells
+        std::vector<float> le, lm;  // the tail's loss
+        dp_source src;
+        T gain, retard, h_sign;
+        float face_e[2], face_h[2]; // gains along a at the box faces: E at lo, hi; H at lo-1, hi
+        float side_h[2], side_e[2]; // gains across: H along h at lo_h-1, hi_h; E along p at lo_p, hi_p
+        float sigma_e, sigma_h, sigma_ha, sigma_ea;
+    };
+    void advance(uint64_t step, std::vector<BoxCorrections<T>> *out);
+    std::vector<Line> lines_;
+    size_t sources_ = 0;
+    float dt_ = 0.0f;
+    uint64_t state_ = 0;        // the lines hold E at state_·dt
+    uint64_t cached_ = ~0ull;
+    std::vector<BoxCorrections<T>> cache_;
+    std::vector<std::pair<uint64_t, std::vector<std::vector<T>>>> checkpoints_;
+    size_t profile_width_ = 0;
 };
 
 // Waveform::evaluate in T (float and double are instantiated).

@@ -82,11 +82,13 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
     if (requested > DP_KERNEL_NAIVE) throw Error(DP_ERR_INVALID, "unknown kernel selector");
     // The fused step stages the coefficient table in shared memory and reads
     // a u8 index through its tensor map: at most 256 materials.
-    const bool fits = tensor_maps_available() && 2 * s.sources.size() <= size_t(kMaxInjections) && s.index_bytes == 1;
+    const bool fits = tensor_maps_available() && s.injection_slots() <= size_t(kMaxInjections) && s.index_bytes == 1;
     if (requested == DP_KERNEL_FUSED && !fits)
-        throw Error(DP_ERR_UNSUPPORTED,
-                    "the fused step takes at most 16 sources and 256 materials (and needs the tensor-map encoder)");
+        throw Error(DP_ERR_UNSUPPORTED, "the fused step takes at most 32 injection slots (2 per source, 8 per "
+                                        "total-field box) and 256 materials (and needs the tensor-map encoder)");
     sim->kernel = (requested == DP_KERNEL_NAIVE || !fits) ? DP_KERNEL_NAIVE : DP_KERNEL_FUSED;
+    sim->lines = IncidentLines<float>(s);
+    if (sim->lines.profile_width()) sim->profile_ring.create(sim->lines.profile_width(), 64);
 
     DeviceScene &d = sim->dev;
     for (int a = 0; a < 3; ++a) d.n[a] = s.grid.n[a];
@@ -201,6 +203,9 @@ dp_status dp_sim_reverse(dp_sim *sim, uint64_t steps) {
     return guarded([&] {
         if (!sim) throw Error(DP_ERR_INVALID, "null handle");
         if (steps == 0) return DP_OK;
+        if (sim->scene.has_boxes())
+            throw Error(DP_ERR_UNSUPPORTED, "a total-field box's incident line absorbs at its far end, so it does not "
+                                            "run backwards");
         if (!sim->scene.reversible)
             throw Error(DP_ERR_LOSSY, "this scene is lossy, and running a dissipative update backwards amplifies "
                                       "roundoff exponentially; reversal needs Boundary::Pec and no conductive material");

@@ -9,6 +9,7 @@
 
 #include "abi.hpp"
 #include "device.cuh"
+#include "profiles.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -62,6 +63,12 @@ struct dp_sim {
     bool accumulating = false;
     uint64_t launches = 0;
     std::vector<StepInjection> injections;
+    // Total-field boxes: their incident lines and the per-step profile values
+    // of the side faces, staged to the device (null when the step has none).
+    IncidentLines<float> lines;
+    ProfileRing<float> profile_ring;
+    std::vector<float> profile_values;
+    const float *step_profiles = nullptr;
     // Probes: Ez and Hy at given cells after every step, in a device ring of
     // probe_capacity steps.  Records are valid for steps after probe_since
     // (a restore, reverse or reset starts a new history).
@@ -87,11 +94,13 @@ struct dp_sim {
 
     FieldSet fields() const { return set[current]; }
 
-    // The non-silent injections of one phase at `time`, in application order
-    // (apply_sources, src/cpu.rs:606-633).
-    void collect(float time, std::vector<DeviceInjection> &out) {
+    // The non-silent injections of step `at_step` (at `time`), in
+    // application order (apply_sources, src/cpu.rs:606-633).
+    void collect(uint64_t at_step, float time, std::vector<DeviceInjection> &out) {
         out.clear();
-        scene.injections(time, injections);
+        const std::vector<BoxCorrections<float>> *boxes = lines.empty() ? nullptr : &lines.at(at_step);
+        scene.injections_in<float>(time, injections, boxes, &profile_values);
+        step_profiles = profile_values.empty() ? nullptr : profile_ring.put(profile_values, stream);
         for (const StepInjection &s : injections) {
             if (s.value == 0.0f) continue;
             DeviceInjection d{};
@@ -103,6 +112,8 @@ struct dp_sim {
             d.magnetic = s.magnetic;
             d.value = s.value;
             d.weight_offset = s.weight_offset;
+            d.profile_offset = s.profile_offset;
+            d.profile_axis = s.profile_axis;
             out.push_back(d);
         }
     }
@@ -110,7 +121,7 @@ struct dp_sim {
     void inject_phase(const std::vector<DeviceInjection> &all, bool magnetic, float sign) {
         for (const DeviceInjection &d : all) {
             if (bool(d.magnetic) != magnetic) continue;
-            launch_inject(dev, fields(), d, sign, stream);
+            launch_inject(dev, fields(), d, sign, step_profiles, stream);
             ++launches;
         }
     }
@@ -122,10 +133,11 @@ struct dp_sim {
             // `E` holds (step + 1)·dt after its update; injections are stated
             // relative to that instant.
             const float time = float(step + 1) * scene.dt;
-            collect(time, all);
+            collect(step, time, all);
             if (kernel == DP_KERNEL_FUSED) {
                 InjectionTable table{};
                 table.count = uint32_t(all.size());
+                table.profiles = step_profiles;
                 for (size_t k = 0; k < all.size(); ++k) table.item[k] = all[k];
                 launch_fused_step(dev, plan, maps[current], set[current ^ 1], accumulating ? intensity : nullptr,
                                   table, error, stream);
@@ -160,7 +172,7 @@ struct dp_sim {
         std::vector<DeviceInjection> all;
         for (uint64_t n = 0; n < steps; ++n) {
             const float time = float(step) * scene.dt;
-            collect(time, all);
+            collect(step - 1, time, all);
             inject_phase(all, false, -1.0f);
             launch_naive_electric(dev, fields(), true, stream);
             ++launches;

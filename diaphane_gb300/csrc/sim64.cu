@@ -8,6 +8,7 @@
 // arithmetic the f32 step's error is stated against.
 #include "abi.hpp"
 #include "device.cuh"
+#include "profiles.hpp"
 
 #include <chrono>
 #include <cstring>
@@ -47,6 +48,10 @@ struct dp_sim64 {
     uint64_t step = 0;
     uint64_t launches = 0;
     std::vector<InjectionOf<double>> injections;
+    IncidentLines<double> lines; // total-field boxes, in double like the drive
+    ProfileRing<double> profile_ring;
+    std::vector<double> profile_values;
+    const double *step_profiles = nullptr;
 
     ~dp_sim64() {
         if (stream) {
@@ -85,7 +90,9 @@ struct dp_sim64 {
             d.component = s.component;
             d.magnetic = s.magnetic;
             d.weight_offset = s.weight_offset;
-            launch_inject(dev, fields, d, s.value, stream);
+            d.profile_offset = s.profile_offset;
+            d.profile_axis = s.profile_axis;
+            launch_inject(dev, fields, d, s.value, step_profiles, stream);
             ++launches;
         }
     }
@@ -94,7 +101,9 @@ struct dp_sim64 {
     void forward(uint64_t steps) {
         for (uint64_t n = 0; n < steps; ++n) {
             const double time = double(step + 1) * double(scene.dt);
-            scene.injections_in<double>(time, injections);
+            const std::vector<BoxCorrections<double>> *boxes = lines.empty() ? nullptr : &lines.at(step);
+            scene.injections_in<double>(time, injections, boxes, &profile_values);
+            step_profiles = profile_values.empty() ? nullptr : profile_ring.put(profile_values, stream);
             launch_naive_magnetic(dev, fields, false, stream);
             inject_phase(true);
             launch_naive_electric(dev, fields, false, stream);
@@ -132,6 +141,8 @@ dp_status dp_sim64_create(const dp_scene *scene, int32_t device, dp_sim64 **out)
         sim->bind();
         check(cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         const Scene &s = sim->scene;
+        sim->lines = IncidentLines<double>(s);
+        if (sim->lines.profile_width()) sim->profile_ring.create(sim->lines.profile_width(), 64);
         const uint64_t cells = s.grid.cells();
         DeviceScene &d = sim->dev;
         for (int a = 0; a < 3; ++a) d.n[a] = s.grid.n[a];

@@ -316,6 +316,8 @@ class Source:
     axis: Axis = Axis.X
     offset: float = 0.0
     waist: float = 0.0
+    box_low: tuple[float, float, float] = (0.0, 0.0, 0.0)
+    box_high: tuple[float, float, float] = (0.0, 0.0, 0.0)
 
     @staticmethod
     def point(at: Sequence[float], polarization: Axis, waveform: Waveform) -> "Source":
@@ -334,12 +336,24 @@ class Source:
     def plane_wave(axis: Axis, offset: float, polarization: Axis, waveform: Waveform) -> "Source":
         return Source(_abi.DP_SOURCE_PLANE_WAVE, polarization, waveform, axis=axis, offset=offset)
 
+    @staticmethod
+    def plane_wave_box(axis: Axis, low: Sequence[float], high: Sequence[float], polarization: Axis,
+                       waveform: Waveform) -> "Source":
+        """A plane wave travelling toward +axis through the total-field box
+        whose corner cells contain `low` and `high` (metres from the domain
+        centre); outside the box every side sees the scattered field alone.
+        An extension: the reference's plane wave spans the whole cross-section
+        (src/source.rs:162-181)."""
+        return Source(_abi.DP_SOURCE_PLANE_WAVE_BOX, polarization, waveform, axis=axis,
+                      box_low=tuple(low), box_high=tuple(high))
+
     def with_amplitude(self, amplitude: float) -> "Source":
         return replace(self, amplitude=amplitude)
 
     def to_c(self) -> _abi.dp_source:
         return _abi.dp_source(self.shape, int(self.polarization), _abi.F3(*self.at), _abi.F3(*self.velocity),
-                              int(self.axis), self.offset, self.waist, self.amplitude, self.waveform.to_c())
+                              int(self.axis), self.offset, self.waist, self.amplitude, self.waveform.to_c(),
+                              _abi.F3(*self.box_low), _abi.F3(*self.box_high))
 
 
 @dataclass(frozen=True)

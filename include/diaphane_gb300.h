@@ -116,19 +116,27 @@ typedef struct dp_waveform {
     float delay;           /* Ricker, Gaussian: seconds */
 } dp_waveform;
 
-enum { DP_SOURCE_POINT = 0, DP_SOURCE_SHEET = 1, DP_SOURCE_PLANE_WAVE = 2 };
+enum { DP_SOURCE_POINT = 0, DP_SOURCE_SHEET = 1, DP_SOURCE_PLANE_WAVE = 2, DP_SOURCE_PLANE_WAVE_BOX = 3 };
 
-/* Source (src/source.rs:136-195). */
+/* Source (src/source.rs:136-195).  DP_SOURCE_PLANE_WAVE_BOX is an extension
+ * the reference does not have: a plane wave travelling toward +axis through a
+ * total-field box, with the scattered field alone outside the box on every
+ * side.  Its incident field is a 1-D Yee line along the travel axis stepped
+ * with the grid's own gains, driven by the plane-wave corrections of
+ * src/source.rs:334-401; the box faces must lie in vacuum.  The batch and
+ * time reversal refuse it (DP_ERR_UNSUPPORTED). */
 typedef struct dp_source {
     uint32_t shape;
     uint32_t polarization; /* driven E component */
     float at[3];           /* point: metres from the domain centre */
     float velocity[3];     /* point: metres per second */
-    uint32_t axis;         /* sheet, plane wave */
+    uint32_t axis;         /* sheet, plane wave, box: travel axis */
     float offset;          /* sheet, plane wave: metres along axis */
     float waist;           /* sheet: metres */
     float amplitude;
     dp_waveform waveform;
+    float box_low[3];      /* box: corners in metres from the domain centre; the */
+    float box_high[3];     /* cells containing them bound the total field */
 } dp_source;
 
 /* Scene (src/scene.rs:116-122).  materials[0] must be vacuum

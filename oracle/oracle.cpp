@@ -35,6 +35,7 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -581,6 +582,183 @@ static std::vector<uint32_t> material_indices(const Grid &grid, const std::vecto
 }
 
 // ---------------------------------------------------------------------------
+// Total-field box (DP_SOURCE_PLANE_WAVE_BOX).  An extension with no reference
+// counterpart: the reference's plane wave (src/source.rs:334-401) spans the
+// whole cross-section.  Restated here from the library's specification, not
+// from its code: a node of the Yee cell is total when its position lies in
+// the box (E_q on lo..hi-1 along q, lo..hi across; H_q the other way round);
+// an update reading across the surface is corrected by its coefficient times
+// the incident value at the node it read, which leaves E_p and H_h on the two
+// faces across the travel axis a and the travel components on the side
+// faces, H_a across h and E_a across p.  The incident field is a 1-D Yee line
+// along a with the grid's gains there, driven by the plane wave's two
+// corrections four cells before the box and ending in a 64-cell graded
+// absorbing tail.  Pinned by the one-way test method of tests/validation.rs:
+// 375-429 (the field outside the box stays at roundoff).
+// ---------------------------------------------------------------------------
+template <typename T> struct BoxSource {
+    struct Face {
+        int component;
+        bool magnetic;
+        size_t origin[3], extent[3];
+        T value;                 // uniform faces
+        std::vector<T> profile;  // side faces: value per cell along a
+    };
+    dp_source src{};
+    int a = 0, p = 0, h = 0;
+    long lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    long first = 0, inject = 0;
+    std::vector<T> e, hf;
+    std::vector<float> ge, gm, le, lm;
+    T gain{}, retard{}, h_sign{};
+    float sigma_e = 1, sigma_h = 1, sigma_ha = 1, sigma_ea = 1;
+    float face_e[2] = {0, 0}, face_h[2] = {0, 0}, side_h[2] = {0, 0}, side_e[2] = {0, 0};
+    std::vector<Face> electric_faces, magnetic_faces;
+
+    BoxSource(const dp_source &s, const Grid &grid) : src(s) {
+        a = int(s.axis);
+        p = int(s.polarization);
+        h = 3 - a - p;
+        if (a == p) panic("a plane wave's polarization must be transverse to its travel");
+        size_t l3[3], h3[3];
+        grid.cell_containing(s.box_low, l3);
+        grid.cell_containing(s.box_high, h3);
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = long(l3[k]);
+            hi[k] = long(h3[k]);
+            if (!(lo[k] >= 1 && lo[k] < hi[k] && hi[k] + 2 <= long(grid.extent[k])))
+                panic("a total-field box needs a cell of scattered field and a wall cell beyond each face");
+        }
+        const std::vector<float> mg_a = grid.magnetic_gains(a), eg_a = grid.electric_gains(a);
+        const std::vector<float> mg_h = grid.magnetic_gains(h), eg_p = grid.electric_gains(p);
+        first = lo[a] - 8;
+        inject = 4;
+        const long last = hi[a] + 8 + 64;
+        const size_t count = size_t(last - first + 1);
+        e.assign(count, T(0));
+        hf.assign(count, T(0));
+        ge.resize(count);
+        gm.resize(count);
+        le.assign(count, 0.0f);
+        lm.assign(count, 0.0f);
+        const long n_a = long(grid.extent[a]);
+        for (size_t i = 0; i < count; ++i) {
+            long c = first + long(i);
+            c = c < 0 ? 0 : (c > n_a - 1 ? n_a - 1 : c);
+            ge[i] = eg_a[size_t(c)];
+            gm[i] = mg_a[size_t(c)];
+        }
+        const float t = 64.0f;
+        const float peak = -(3.0f + 1.0f) * std::log(1e-6f) * grid.courant / (4.0f * t);
+        const long tail0 = long(count) - 64;
+        for (long i = tail0; i < long(count); ++i) {
+            const float de = std::fmin(float(i - tail0 + 1) / t, 1.0f);
+            const float dh = std::fmin((float(i - tail0) + 1.5f) / t, 1.0f);
+            le[size_t(i)] = peak * de * de * de;
+            lm[size_t(i)] = peak * dh * dh * dh;
+        }
+        const float spacing = grid.spacing[a].finest();
+        const T dt = T(grid.time_step());
+        gain = T(SPEED_OF_LIGHT * grid.time_step() / spacing);
+        const T omega = T(2) * Math<T>::pi * T(s.waveform.frequency);
+        retard = std::asin(Math<T>::sin(T(0.5) * omega * dt) / gain) / omega;
+        h_sign = ((p + 1) % 3) == a ? T(-1) : T(1);
+        sigma_e = (p + 1) % 3 == a ? 1.0f : -1.0f;
+        sigma_h = (h + 1) % 3 == a ? 1.0f : -1.0f;
+        sigma_ha = (a + 2) % 3 == p ? 1.0f : -1.0f;
+        sigma_ea = (a + 2) % 3 == h ? 1.0f : -1.0f;
+        face_e[0] = eg_a[size_t(lo[a])];
+        face_e[1] = eg_a[size_t(hi[a])];
+        face_h[0] = mg_a[size_t(lo[a] - 1)];
+        face_h[1] = mg_a[size_t(hi[a])];
+        side_h[0] = mg_h[size_t(lo[h] - 1)];
+        side_h[1] = mg_h[size_t(hi[h])];
+        side_e[0] = eg_p[size_t(lo[p])];
+        side_e[1] = eg_p[size_t(hi[p])];
+    }
+
+    T E(long cell) const { return e[size_t(cell - first)]; }
+    T H(long cell) const { return hf[size_t(cell - first)]; }
+
+    Face face(int component, bool magnetic) const {
+        Face f{};
+        f.component = component;
+        f.magnetic = magnetic;
+        f.origin[a] = size_t(lo[a]);
+        f.extent[a] = size_t(hi[a] - lo[a]);
+        f.origin[p] = size_t(lo[p]);
+        f.extent[p] = size_t(hi[p] - lo[p]);
+        f.origin[h] = size_t(lo[h]);
+        f.extent[h] = size_t(hi[h] - lo[h] + 1);
+        return f;
+    }
+
+    // From the incident E at this step's start: H_h across a, H_a across h.
+    void magnetic_corrections() {
+        magnetic_faces.clear();
+        for (int f = 0; f < 2; ++f) {
+            Face c = face(h, true);
+            c.origin[a] = size_t(f ? hi[a] : lo[a] - 1);
+            c.extent[a] = 1;
+            c.value = T(sigma_h * (f ? -face_h[1] : face_h[0])) * E(f ? hi[a] : lo[a]);
+            magnetic_faces.push_back(c);
+        }
+        for (int f = 0; f < 2; ++f) {
+            Face c = face(a, true);
+            c.extent[a] = size_t(hi[a] - lo[a] + 1);
+            c.origin[h] = size_t(f ? hi[h] : lo[h] - 1);
+            c.extent[h] = 1;
+            c.value = T(1);
+            const T coef = T(sigma_ha * (f ? -side_h[1] : side_h[0]));
+            for (long x = lo[a]; x <= hi[a]; ++x) c.profile.push_back(coef * E(x));
+            magnetic_faces.push_back(c);
+        }
+    }
+
+    // The line's H (the grid's update of a uniform wave), then its drive.
+    void step_h(T time, T dt) {
+        const size_t count = e.size();
+        for (size_t i = 0; i < count; ++i) {
+            const T next = i + 1 < count ? e[i + 1] : T(0);
+            const T curl = T(sigma_h) * (T(gm[i]) * (next - e[i]));
+            const T loss = T(lm[i]);
+            hf[i] = loss == T(0) ? hf[i] - curl : ((T(1) - loss) * hf[i] - curl) / (T(1) + loss);
+        }
+        hf[size_t(inject - 1)] += h_sign * gain * (T(src.amplitude) * evaluate<T>(src.waveform, time - dt));
+    }
+
+    // From the incident H at the half step: E_p across a, E_a across p.
+    void electric_corrections() {
+        electric_faces.clear();
+        for (int f = 0; f < 2; ++f) {
+            Face c = face(p, false);
+            c.origin[a] = size_t(f ? hi[a] : lo[a]);
+            c.extent[a] = 1;
+            c.value = T(sigma_e * (f ? face_e[1] : -face_e[0])) * H(f ? hi[a] : lo[a] - 1);
+            electric_faces.push_back(c);
+        }
+        for (int f = 0; f < 2; ++f) {
+            Face c = face(a, false);
+            c.origin[p] = size_t(f ? hi[p] : lo[p]);
+            c.extent[p] = 1;
+            c.value = T(1);
+            const T coef = T(sigma_ea * (f ? side_e[1] : -side_e[0]));
+            for (long x = lo[a]; x < hi[a]; ++x) c.profile.push_back(coef * H(x));
+            electric_faces.push_back(c);
+        }
+    }
+
+    void step_e(T time, T dt) {
+        for (size_t i = 1; i < e.size(); ++i) {
+            const T curl = T(sigma_e) * (T(ge[i]) * (hf[i] - hf[i - 1]));
+            const T loss = T(le[i]);
+            e[i] = loss == T(0) ? e[i] + curl : ((T(1) - loss) * e[i] + curl) / (T(1) + loss);
+        }
+        e[size_t(inject)] += gain * (T(src.amplitude) * evaluate<T>(src.waveform, time - T(0.5) * dt + retard));
+    }
+};
+
+// ---------------------------------------------------------------------------
 // Simulation — src/cpu.rs:65-713
 // ---------------------------------------------------------------------------
 struct SimBase {
@@ -599,6 +777,7 @@ template <typename T> struct Simulation : SimBase {
     bool accumulating = false;
     uint64_t accumulated = 0;
     std::vector<dp_source> sources;
+    std::vector<std::shared_ptr<BoxSource<T>>> boxes; // per source; null unless a total-field box
     uint64_t step = 0;
     int threads = 1;
 
@@ -611,6 +790,8 @@ template <typename T> struct Simulation : SimBase {
         for (const auto &s : shapes)
             if (s.material >= d.material_count) panic("a shape refers to a missing material");
         sources.assign(d.sources, d.sources + d.source_count);
+        for (const auto &src : sources)
+            boxes.push_back(src.shape == DP_SOURCE_PLANE_WAVE_BOX ? std::make_shared<BoxSource<T>>(src, grid) : nullptr);
         size_t total = grid.total();
         for (int a = 0; a < 3; ++a) {
             electric[a].assign(total, T(0));
@@ -640,6 +821,8 @@ template <typename T> struct Simulation : SimBase {
         std::fill(intensity.begin(), intensity.end(), T(0));
         accumulated = 0;
         step = 0;
+        for (auto &b : boxes)
+            if (b) b = std::make_shared<BoxSource<T>>(b->src, grid);
     }
 
     // src/cpu.rs:174-198
@@ -647,10 +830,20 @@ template <typename T> struct Simulation : SimBase {
         // `(step + 1) as f32 * time_step()` in f32; exact in the f64 instance.
         T time = std::is_same_v<T, float> ? T(static_cast<float>(step + 1) * grid.time_step())
                                           : T(double(step + 1) * double(grid.time_step()));
+        const T dt = T(grid.time_step());
+        for (auto &b : boxes)
+            if (b) b->magnetic_corrections();
         update_magnetic(false);
         apply_sources(time, T(1), true);
+        for (auto &b : boxes)
+            if (b) {
+                b->step_h(time, dt);
+                b->electric_corrections();
+            }
         update_electric(false);
         apply_sources(time, T(1), false);
+        for (auto &b : boxes)
+            if (b) b->step_e(time, dt);
         if (accumulating) {
             const long n = long(intensity.size());
 #pragma omp parallel for schedule(static) num_threads(threads)
@@ -666,6 +859,8 @@ template <typename T> struct Simulation : SimBase {
 
     // src/cpu.rs:253-273
     void reverse() {
+        for (const auto &b : boxes)
+            if (b) panic("a total-field box's incident line absorbs at its far end, so it does not run backwards");
         if (!is_reversible()) panic("this scene is lossy, and running a dissipative update backwards amplifies roundoff");
         if (step == 0) panic("cannot step back past the start");
         clear_intensity();
@@ -815,7 +1010,12 @@ template <typename T> struct Simulation : SimBase {
 
     // apply_sources — src/cpu.rs:606-633
     void apply_sources(T time, T sign, bool magnetic_phase) {
-        for (const auto &source : sources) {
+        for (size_t k = 0; k < sources.size(); ++k) {
+            const dp_source &source = sources[k];
+            if (boxes[k]) {
+                apply_box(*boxes[k], magnetic_phase);
+                continue;
+            }
             Injection<T> inj[2];
             injections<T>(source, grid, time, inj);
             for (const auto &injection : inj) {
@@ -834,6 +1034,38 @@ template <typename T> struct Simulation : SimBase {
                                 value * T(injection.weight(position));
                         }
             }
+        }
+    }
+
+    // Total-field boxes' incident lines brought to `target` steps from the
+    // start (their state depends on the step count alone).
+    void seek_boxes(uint64_t target) {
+        const T dt = T(grid.time_step());
+        for (auto &b : boxes) {
+            if (!b) continue;
+            b = std::make_shared<BoxSource<T>>(b->src, grid);
+            for (uint64_t n = 0; n < target; ++n) {
+                const T time = std::is_same_v<T, float> ? T(static_cast<float>(n + 1) * grid.time_step())
+                                                        : T(double(n + 1) * double(grid.time_step()));
+                b->step_h(time, dt);
+                b->step_e(time, dt);
+            }
+        }
+    }
+
+    // A box's corrections of one phase: a uniform face adds value · 1 (skipped
+    // when zero, as any injection), a side face its profile value · 1.
+    void apply_box(const BoxSource<T> &b, bool magnetic_phase) {
+        for (const auto &f : magnetic_phase ? b.magnetic_faces : b.electric_faces) {
+            if (f.profile.empty() && f.value == T(0)) continue;
+            T *target = f.magnetic ? magnetic[f.component].data() : electric[f.component].data();
+            for (size_t dz = 0; dz < f.extent[2]; ++dz)
+                for (size_t dy = 0; dy < f.extent[1]; ++dy)
+                    for (size_t dx = 0; dx < f.extent[0]; ++dx) {
+                        const size_t c[3] = {f.origin[0] + dx, f.origin[1] + dy, f.origin[2] + dz};
+                        const T w = f.profile.empty() ? T(1.0f) : f.profile[c[b.a] - f.origin[b.a]];
+                        target[grid.index(c[0], c[1], c[2])] += f.value * w;
+                    }
         }
     }
 
@@ -1031,6 +1263,7 @@ int or_sim_restore(or_sim *s, uint64_t step, const float *electric, const float 
                 sim->magnetic[a][i] = magnetic[a * n + i];
             }
         sim->step = step;
+        sim->seek_boxes(step);
     };
     if (s->f32) restore(s->f32);
     else restore(s->f64);
@@ -1131,6 +1364,7 @@ int or_sim_injections(const or_sim *s, float time, dp_injection *out, uint32_t c
     const auto &sim = *s->f32;
     uint32_t n = 0;
     for (const auto &src : sim.sources) {
+        if (src.shape == DP_SOURCE_PLANE_WAVE_BOX) return 1; // depends on its line's history, not on time alone
         Injection<float> inj[2];
         injections<float>(src, sim.grid, time, inj);
         for (const auto &i : inj) {

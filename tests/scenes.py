@@ -93,6 +93,33 @@ def free_flight(side: int = 80):
     return scene
 
 
+def box_wave():
+    """A total-field box (an extension of the reference's plane wave) 14 cells
+    in from every wall of a 60×48×44 absorbing grid, x-travelling and
+    z-polarized, with a dielectric sphere and a conductor inside it: the wave
+    crosses the box, the scatterers' field leaves it on every side."""
+    scene = Scene.empty(Extent(60, 48, 44), 1e-3)
+    frequency = scene.grid.frequency_for_resolution(10.0)
+    n = (60, 48, 44)
+
+    def metres(axis: int, cell: int) -> float:
+        return (cell + 0.5) * 1e-3 - n[axis] * 1e-3 / 2.0
+
+    glass = scene.materials.push(Material.refractive(1.5))
+    metal = scene.materials.push(Material.PERFECT_CONDUCTOR)
+    scene.shapes.append(Shape.sphere((-3e-3, 1e-3, 0.0), 6e-3, glass))
+    scene.shapes.append(Shape.sphere((8e-3, -4e-3, 2e-3), 3e-3, metal))
+    low = tuple(metres(a, 14) for a in range(3))
+    high = tuple(metres(a, n[a] - 15) for a in range(3))
+    scene.sources.append(Source.plane_wave_box(Axis.X, low, high, Axis.Z, Waveform.gaussian_pulse(frequency, 3.0)))
+    return scene, 220
+
+
+def has_box(scene) -> bool:
+    from diaphane_gb300 import _abi
+    return any(s.shape == _abi.DP_SOURCE_PLANE_WAVE_BOX for s in scene.sources)
+
+
 PARITY_CASES = {
     "photon": photon,
     "cavity": cavity,
@@ -101,4 +128,5 @@ PARITY_CASES = {
     "graded": graded,
     "graded_aligned": graded_aligned,
     "plane_wave": plane_wave,
+    "box_wave": box_wave,
 }

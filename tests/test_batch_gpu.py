@@ -60,6 +60,7 @@ def test_scenes_that_join_and_leave_between_chunks(threads):
 
 def test_the_parity_scenes_in_one_batch(threads):
     cases = {name: make() for name, make in scenes.PARITY_CASES.items()}
+    cases = {name: case for name, case in cases.items() if not scenes.has_box(case[0])}
     batch = Batch(ARENA, chunk_steps=50, max_scenes=16)
     ids = {name: batch.add(ResolvedScene(scene), steps) for name, (scene, steps) in cases.items()}
     batch.run_to_completion()
@@ -120,3 +121,12 @@ def test_reads_into_a_caller_buffer_match_fresh_arrays():
             assert into.size == fresh.size and np.shares_memory(into, pinned)
             assert np.array_equal(bits(into), bits(fresh))
             assert np.array_equal(bits(read_solo(out=pinned)), bits(fresh))
+
+
+def test_a_total_field_box_is_refused_by_the_batch():
+    from diaphane_gb300 import _abi
+    scene, steps = scenes.box_wave()
+    batch = Batch(ARENA, chunk_steps=16, max_scenes=4)
+    with pytest.raises(Exception) as failure:
+        batch.add(ResolvedScene(scene), steps)
+    assert failure.value.status == _abi.DP_ERR_UNSUPPORTED

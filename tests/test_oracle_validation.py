@@ -348,3 +348,44 @@ def test_a_graded_conducting_box_conserves_energy():
     # The reference asserts < 1e-3 (its documentation quotes 4.9e-4; the
     # oracle measures 2.4e-4 while reproducing the other published figures).
     assert drift < 1e-3
+
+
+# ---- total-field box (an extension; pinned by the one-way method above) ---------------
+
+def box_scene(travel: Axis, polarization: Axis, n: int = 48, lo: int = 14, hi: int = 34) -> Scene:
+    """A vacuum cube with a total-field box whose faces sit at cells lo and
+    hi on every axis, a Gaussian pulse at 20 cells per wavelength."""
+    scene = Scene.empty(Extent.cube(n), 1e-3)
+    frequency = scene.grid.frequency_for_resolution(20.0)
+
+    def metres(cell: int) -> float:
+        return (cell + 0.5) * 1e-3 - n * 1e-3 / 2.0
+
+    scene.sources.append(Source.plane_wave_box(travel, (metres(lo),) * 3, (metres(hi),) * 3, polarization,
+                                               Waveform.gaussian_pulse(frequency, 4.0)))
+    return scene
+
+
+@pytest.mark.parametrize("travel,polarization", [(Axis.X, Axis.Z), (Axis.X, Axis.Y), (Axis.Y, Axis.X),
+                                                 (Axis.Y, Axis.Z), (Axis.Z, Axis.X), (Axis.Z, Axis.Y)])
+def test_a_total_field_box_keeps_its_wave_inside(travel, polarization):
+    # The reference's one-way measurement (tests/validation.rs:375-429) over
+    # every side of the box: the wave crosses the total field at full
+    # strength while everything outside stays at roundoff, because the
+    # incident line propagates exactly what the grid does, dispersion
+    # included, and each face subtracts it where the stencil reaches across.
+    n, lo, hi = 48, 14, 34
+    sim = sim_of(box_scene(travel, polarization, n, lo, hi))
+    inside = np.zeros((n, n, n), dtype=bool)
+    inside[lo:hi + 1, lo:hi + 1, lo:hi + 1] = True
+    total_peak = scattered_peak = 0.0
+    for step in range(320):
+        sim.advance()
+        if step % 4:
+            continue
+        e = [sim.electric(a).reshape(n, n, n) for a in (Axis.X, Axis.Y, Axis.Z)]
+        total_peak = max(total_peak, float(np.abs(e[int(polarization)][inside]).max()))
+        scattered_peak = max(scattered_peak, max(float(np.abs(c[~inside]).max()) for c in e))
+    assert 0.8 <= total_peak < 1.25, total_peak
+    leak = 20.0 * math.log10(max(scattered_peak, 1e-30) / total_peak)
+    assert leak < -80.0, f"the box leaks {leak:.1f} dB"

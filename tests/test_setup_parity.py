@@ -38,7 +38,7 @@ def test_tables_match_the_oracle_bit_for_bit(name):
     assert np.float32(product.absorber_peak) == np.float32(reference.absorber_peak())
 
 
-@pytest.mark.parametrize("name", sorted(all_scenes()))
+@pytest.mark.parametrize("name", sorted(n for n, s in all_scenes().items() if not scenes.has_box(s)))
 def test_injections_match_the_oracle_at_every_step(name):
     scene = all_scenes()[name]
     product = ResolvedScene(scene)
@@ -128,3 +128,13 @@ def test_world_to_cell_lookup_matches_the_oracles_coordinate_map(case):
         for a in range(3):
             expected[a * samples + k] = cell[a]
     assert np.array_equal(ours.view(np.uint32), expected.view(np.uint32))
+
+
+def test_a_total_field_box_is_not_a_function_of_time_alone():
+    # Its corrections come from the incident line's history, so the
+    # stateless per-time query refuses it on both sides.
+    scene, _ = scenes.box_wave()
+    with pytest.raises(Exception):
+        ResolvedScene(scene).injections(1e-12)
+    with pytest.raises(Exception):
+        oracle.OracleSimulation(scene).injections(1e-12)
