@@ -88,7 +88,7 @@ def profiled_traffic(side: int) -> float | None:
 def config(side: int, n: int) -> dict:
     return {"workload": WORKLOAD if side == 512 else f"heterogeneous scatterers {side}^3",
             "grid": [side, side, side], "spheres": 200, "materials": 203, "intensity": True,
-            "source": "TFSF plane wave, x-travelling, 26 cells from the low wall",
+            "source": "TFSF box 16 cells inside the absorber (faces at cells 26 and 485), x-travelling plane wave",
             "boundary": "absorbing, 10 cells",
             "l2": f"inputs larger than L2 (fields {48 * side ** 3 / 1e9:.2f} GB per step), no flush",
             "parallelism": f"replicas{n}"}

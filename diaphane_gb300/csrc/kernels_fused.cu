@@ -78,7 +78,8 @@ template <int CX, int TY, int SLOTS> struct Geometry {
     static constexpr int kCompactItems = CX == 1 ? 64 : 96;
     static constexpr int SCRATCH_OFF = (BAR_OFF + kSlots * 8 + 15) & ~15;
     static constexpr int SCRATCH_WARP = 2 * kCompactItems * 4;
-    static constexpr int SMEM = SCRATCH_OFF + kWarps * SCRATCH_WARP;
+    static constexpr int INJ_OFF = SCRATCH_OFF + kWarps * SCRATCH_WARP; // 16-aligned
+    static constexpr int SMEM = INJ_OFF + kMaxInjections * int(sizeof(DeviceInjection));
 };
 
 struct FusedArgs {
@@ -260,9 +261,11 @@ __device__ __forceinline__ void divide_compacted(float *scratch, int items_max, 
     }
 }
 
-// Bit k is set when injection k of `magnetic` phase covers row y and any of
-// the cells [xa, xb).  Computed once per thread; the per-plane test is then a
-// single z comparison per set bit.
+// Bit k is set when injection k of `magnetic` phase covers row y, any of the
+// cells [xa, xb) and any of the planes [za, zb) the thread will compute.
+// Computed once per thread; the per-plane test is then a single z comparison
+// per set bit, and a one-plane face (a total-field box's) costs nothing to the
+// units that do not reach its plane.
 // The injections of one step as the kernel reads them: a table in kernel
 // parameters (one scene) or in global memory (a batch).
 struct InjectionView {
@@ -271,12 +274,14 @@ struct InjectionView {
     const float *profiles; // total-field box profile values of the step, or null
 };
 
-__device__ __forceinline__ uint32_t injection_mask(const InjectionView &t, bool magnetic, int xa, int xb, int y) {
+__device__ __forceinline__ uint32_t injection_mask(const InjectionView &t, bool magnetic, int xa, int xb, int y,
+                                                   int za, int zb) {
     uint32_t m = 0;
     for (uint32_t k = 0; k < t.count; ++k) {
         const DeviceInjection &d = t.item[k];
         if (d.magnetic == uint32_t(magnetic) && y >= int(d.origin[1]) && y < int(d.origin[1] + d.extent[1]) &&
-            xb > int(d.origin[0]) && xa < int(d.origin[0] + d.extent[0]))
+            xb > int(d.origin[0]) && xa < int(d.origin[0] + d.extent[0]) && zb > int(d.origin[2]) &&
+            za < int(d.origin[2] + d.extent[2]))
             m |= 1u << k;
     }
     return m;
@@ -294,6 +299,22 @@ __device__ __forceinline__ void apply_injections(const InjectionView &t, const f
         const int dz = z - int(d.origin[2]);
         if (dz < 0 || dz >= int(d.extent[2])) continue;
         const int dy = y - int(d.origin[1]);
+        if (d.weight_offset < 0 && d.profile_offset < 0) {
+            // Weight 1 everywhere (a point, a plane, a box's uniform face):
+            // value * 1 is value, so each covered cell just adds it.
+            const int dx0 = x - int(d.origin[0]);
+            const uint32_t ex = d.extent[0], c = d.component;
+            const float add = d.value;
+#pragma unroll
+            for (int j = 0; j < CX; ++j) {
+                // Selects, not an added zero: -0 + 0 would turn a cell's -0 into +0.
+                const bool in = uint32_t(dx0 + j) < ex;
+                f0.v[j] = (in && c == 0) ? f0.v[j] + add : f0.v[j];
+                f1.v[j] = (in && c == 1) ? f1.v[j] + add : f1.v[j];
+                f2.v[j] = (in && c == 2) ? f2.v[j] + add : f2.v[j];
+            }
+            continue;
+        }
 #pragma unroll
         for (int j = 0; j < CX; ++j) {
             const int dx = x + j - int(d.origin[0]);
@@ -362,7 +383,10 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
     constexpr int kWarps = G::kWarps, kThreads = G::kThreads, kSlots = G::kSlots;
     extern __shared__ __align__(128) unsigned char smem[];
     const DeviceScene &s = u.s;
-    const InjectionView &inj = u.inj;
+    // The step's injections, staged in shared memory below with the
+    // coefficient table: the per-plane tests and additions read them there.
+    DeviceInjection *inj_staged = reinterpret_cast<DeviceInjection *>(smem + G::INJ_OFF);
+    const InjectionView inj{inj_staged, u.inj.count, u.inj.profiles};
     const int nx = int(s.n[0]), ny = int(s.n[1]);
     const uint64_t pitch = s.pitch;
     const uint64_t cells = s.cells;
@@ -396,6 +420,13 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         for (int p = zs; p <= min(zs + kSlots - 1, last_plane); ++p) issue(p);
     }
     for (int m = threadIdx.x; m < kMaxMaterials; m += kThreads) coeff[m] = __ldg(&s.coeff[m]);
+    {
+        constexpr int kWords = int(sizeof(DeviceInjection) / 4);
+        const uint32_t *from = reinterpret_cast<const uint32_t *>(u.inj.item);
+        uint32_t *to = reinterpret_cast<uint32_t *>(inj_staged);
+        const int words = int(u.inj.count) * kWords;
+        for (int w = threadIdx.x; w < words; w += kThreads) to[w] = from[w];
+    }
     __syncthreads();
 
     // Per-thread constants: this lane's cells along x, this warp's row.
@@ -416,8 +447,8 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
     // the grid) are computed but never stored.
     const int full_lane = nx - xl >= CX ? CX : nx - xl;
     const bool has_inj = inj.count != 0;
-    const uint32_t mask_h = has_inj ? injection_mask(inj, true, xl, xl + CX, y) : 0u;
-    const uint32_t mask_e = has_inj ? injection_mask(inj, false, xl, xl + CX, y) : 0u;
+    const uint32_t mask_h = has_inj ? injection_mask(inj, true, xl, xl + CX, y, zs, z1) : 0u;
+    const uint32_t mask_e = has_inj ? injection_mask(inj, false, xl, xl + CX, y, zs, z1) : 0u;
 
     // Halo cells, packed onto the first warps: halo index i = 32·warp + lane;
     // i < TX takes cell x0+i of row y0-1 (the Hx, Hz that E at row y0 reads),
@@ -448,7 +479,7 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         hc.mgy = ldg_at(s.mgain + nx, hc.y, ny);
         hc.aiy = ldg_at(absorb_int + nx, hc.y, ny);
         hc.ahy = ldg_at(absorb_half + nx, hc.y, ny);
-        hc.mask = has_inj ? injection_mask(inj, true, hc.x, hc.x + 1, hc.y) : 0u;
+        hc.mask = has_inj ? injection_mask(inj, true, hc.x, hc.x + 1, hc.y, zs, z1) : 0u;
     }
 
     float *scratch = reinterpret_cast<float *>(smem + G::SCRATCH_OFF + warp * G::SCRATCH_WARP);

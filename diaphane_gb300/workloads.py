@@ -39,18 +39,20 @@ def heterogeneous(side: int = 512, spheres: int = 200, seed: int = HETEROGENEOUS
     """Heterogeneous scatterers on a uniform side³ grid at 1 mm.
 
     * 10-cell absorbing layer (R0 = 1e-6).
+    * A total-field box 16 cells inside the absorber on every side (faces at
+      cells 26 and side-27; fewer cells on grids too small for that) through
+      which an x-travelling, z-polarized plane wave passes; outside it every
+      side sees the scattered field alone.  Gaussian pulse, 3 cycles, at the
+      frequency whose wavelength is 10 cells.
     * `spheres` dielectric spheres, radius uniform in [4, 24] cells, εr
-      uniform in [1, 4], centres uniform over the interior but kept two cells
-      clear of the absorber and of the plane-wave correction rows (which must
-      be vacuum, src/source.rs:177-180).  Each sphere is its own material.
+      uniform in [1, 4], centres uniform over the box's interior, kept two
+      cells clear of its faces (which must lie in vacuum).  Each sphere is
+      its own material.
     * One perfectly conducting sphere of radius 40 cells at the centre.
     * One lossy slab, Material::matched_lossy(2, σ), 16 cells thick across x
-      at 3/4 of the domain, with σ chosen so the electric half-step loss
+      at 3/4 of the domain and spanning the box's cross-section two cells
+      short of its faces, with σ chosen so the electric half-step loss
       σ·Δt/(2ε0εr) is 0.02; matched magnetic loss keeps it reflectionless.
-    * An x-travelling, z-polarized plane wave (total-field/scattered-field,
-      src/source.rs:334-401) entering 16 cells inside the absorber, i.e. 26
-      cells from the low x wall; Gaussian pulse, 3 cycles, at the frequency
-      whose wavelength is 10 cells.
     Painted in that order: spheres, then the conductor, then the slab.
     """
     rng = SplitMix64(seed)
@@ -58,33 +60,39 @@ def heterogeneous(side: int = 512, spheres: int = 200, seed: int = HETEROGENEOUS
     scene = Scene.empty(Extent.cube(side), float(cell))
     grid = scene.grid
     half = side * float(cell) / 2.0
-    absorber, inset = 10, 16
-    plane_cell = absorber + inset
+    absorber = 10
+    inset = min(16, max(2, (side - 2 * absorber) // 6))
+    lo = max(1, min(absorber + inset, side // 2 - 3))  # the box's faces, in cells
+    hi = side - 1 - lo
+    largest = max(1.0, min(24.0, (hi - lo) / 2.0 - 3.0))
 
     def position(c: float) -> float:
         return float(f32(c) * cell - f32(half))
 
     for _ in range(spheres):
-        r = rng.uniform(4.0, 24.0)
+        r = min(rng.uniform(4.0, 24.0), largest)
         eps = rng.uniform(1.0, 4.0)
-        lo_x, hi_x = plane_cell + 2 + r, side - absorber - 2 - r
-        lo, hi = absorber + 2 + r, side - absorber - 2 - r
-        cx, cy, cz = rng.uniform(lo_x, hi_x), rng.uniform(lo, hi), rng.uniform(lo, hi)
+        c_lo, c_hi = lo + 2 + r, hi - 2 - r
+        cx, cy, cz = rng.uniform(c_lo, c_hi), rng.uniform(c_lo, c_hi), rng.uniform(c_lo, c_hi)
         m = scene.materials.push(Material.dielectric(eps))
         scene.shapes.append(Shape.sphere((position(cx), position(cy), position(cz)), float(f32(r) * cell), m))
 
     pec = scene.materials.push(Material.PERFECT_CONDUCTOR)
-    scene.shapes.append(Shape.sphere((0.0, 0.0, 0.0), float(f32(40.0) * cell), pec))
+    scene.shapes.append(Shape.sphere((0.0, 0.0, 0.0), float(f32(min(40.0, largest)) * cell), pec))
 
     dt = grid.time_step()
     eps_slab = 2.0
     sigma = 0.02 * 2.0 * 8.854188e-12 * eps_slab / dt
     lossy = scene.materials.push(Material.matched_lossy(eps_slab, sigma))
-    scene.shapes.append(Shape.slab(Axis.X, position(0.75 * side), float(f32(16.0) * cell), lossy))
+    thickness = max(1, min(16, (hi - lo) // 4))
+    slab_x = min(0.75 * side, hi - 2 - thickness / 2.0)
+    across = float(f32(max(1, hi - lo - 4)) * cell)
+    scene.shapes.append(Shape.block((position(slab_x), 0.0, 0.0), (float(f32(thickness) * cell), across, across),
+                                    lossy))
 
     frequency = grid.frequency_for_resolution(10.0)
-    scene.sources.append(Source.plane_wave(Axis.X, position(plane_cell + 0.5), Axis.Z,
-                                           Waveform.gaussian_pulse(frequency, 3.0)))
+    low, high = (position(lo + 0.5),) * 3, (position(hi + 0.5),) * 3
+    scene.sources.append(Source.plane_wave_box(Axis.X, low, high, Axis.Z, Waveform.gaussian_pulse(frequency, 3.0)))
     return scene
 
 
