@@ -72,3 +72,19 @@ def test_the_box_does_not_run_backwards():
         sim.reverse_by(1)
     assert failure.value.status == _abi.DP_ERR_UNSUPPORTED
 
+
+
+def test_a_restore_replays_from_a_line_checkpoint():
+    # 700 steps leave checkpoints at 256 and 512; restoring to step 300
+    # replays the line from 256, not from the start.
+    scene, _ = scenes.box_wave()
+    straight = Simulation(scene)
+    straight.advance_by(700)
+    sim = Simulation(scene)
+    sim.advance_by(300)
+    snap = sim.snapshot()
+    sim.advance_by(400)
+    sim.restore(snap)
+    sim.advance_by(400)
+    assert np.array_equal(bits(sim.read_electric()), bits(straight.read_electric()))
+    assert np.array_equal(bits(sim.read_magnetic()), bits(straight.read_magnetic()))
