@@ -55,7 +55,8 @@ def parse():
     p.add_argument("--variant", default="", help="fused kernel cx,tile_y,slots (default: tuned)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the mixed-size batch measurement")
-    p.add_argument("--workload", choices=["heterogeneous", "batched", "served", "accuracy", "extras"], default="heterogeneous")
+    p.add_argument("--workload", choices=["heterogeneous", "batched", "served", "accuracy", "extras", "kernels"],
+                   default="heterogeneous")
     p.add_argument("--scenes", type=int, default=256, help="batched: scenes per batch")
     p.add_argument("--batch-steps", type=int, default=1000, help="batched: steps per scene")
     p.add_argument("--rates", default="4,16,64", help="served: arrival rates to sweep, requests/s")
@@ -621,6 +622,54 @@ def extras_measurement(side: int = 256, device: int = 0) -> dict:
     return out
 
 
+def kernels_measurement(side: int = 256, device: int = 0) -> dict:
+    """Every kernel around the fused step, a few launches each on the
+    heterogeneous scene at side³, for a launch list with DRAM counters: the
+    rasterizer, the one-thread-per-cell passes (H, E, each injection,
+    intensity) in f32 and in f64, the energy, finiteness and energy-density
+    reductions, the probe gather, row packing for a grid whose rows are
+    padded, the renderer's reduction and ray march, and the batch's probe
+    gather.  Wall times are reported; the per-kernel figures come from ncu."""
+    import torch
+    from diaphane_gb300 import (DP_KERNEL_NAIVE, Batch, ResolvedScene, Simulation, Simulation64, workloads)
+    from diaphane_gb300.render import Renderer
+    t0 = time.perf_counter()
+    resolved = ResolvedScene(workloads.heterogeneous(side))
+    index = torch.empty(resolved.cells, dtype=torch.uint8, device=f"cuda:{device}")
+    resolved.rasterize(index.data_ptr())
+    sim = Simulation(resolved, kernel=DP_KERNEL_NAIVE, device=device)
+    sim.set_accumulate_intensity(True)
+    sim.set_probes([(side // 2, side // 2, k * side // 8) for k in range(8)], 64)
+    sim.advance_by(3)
+    sim.energy()
+    sim.is_finite()
+    sim.energy_density()
+    renderer = Renderer(sim, 1280, 720)
+    renderer.measure()
+    renderer.draw()
+    sim.wait()
+    renderer.close()
+    sim.close()
+    fp64 = Simulation64(resolved, device=device)
+    fp64.advance_by(2)
+    fp64.energy()
+    fp64.close()
+    odd = ResolvedScene(workloads.heterogeneous(side - 2))  # rows padded from side-2 to side cells
+    padded = Simulation(odd, device=device)
+    padded.advance_by(2)
+    padded.write_electric(padded.read_electric())
+    padded.close()
+    small = [ResolvedScene(workloads.mixed_scene(BATCH_SEED + k)) for k in range(4)]
+    batch = Batch(int(1.05 * sum(Batch.bytes_for(r, 4) for r in small)) + (64 << 20), chunk_steps=4,
+                  max_scenes=4, device=device)
+    for r in small:
+        batch.add(r, 4, probes=[(4, 4, 4), (8, 8, 8)])
+    batch.run_to_completion()
+    batch.close()
+    torch.cuda.synchronize(device)
+    return {"side": side, "seconds": time.perf_counter() - t0}
+
+
 def run_accuracy(args):
     from diaphane_gb300 import workloads
     cases = [accuracy_case("free flight 80^3", workloads.free_flight(80), 1000),
@@ -644,6 +693,10 @@ def main():
     elif args.workload == "extras":
         line = {"metric": "costs around the step", "workload": "extras"}
         line.update(extras_measurement(args.side if args.side != 512 else 256))
+        print(json.dumps(line), flush=True)
+    elif args.workload == "kernels":
+        line = {"metric": "every kernel around the fused step, for ncu", "workload": "kernels"}
+        line.update(kernels_measurement(args.side if args.side != 512 else 256))
         print(json.dumps(line), flush=True)
     else:
         run_ours(args)

@@ -193,11 +193,19 @@ __global__ void __launch_bounds__(kThreads) energy_density_pass(DeviceScene s, F
 }
 
 // is_finite (src/cpu.rs:707-713): any non-finite value clears the flag.
+// 16-byte loads (the field sets are 16-byte aligned), the few values past the
+// last whole quad checked one by one.
 __global__ void __launch_bounds__(kThreads) finite_pass(DeviceScene s, FieldSet f, int32_t *flag) {
-    const uint64_t total = 3 * s.cells;
+    const uint64_t total = 3 * s.cells, quads = total / 4;
+    const float4 *e = reinterpret_cast<const float4 *>(f.e), *h = reinterpret_cast<const float4 *>(f.h);
     bool ok = true;
-    for (uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x; i < total; i += uint64_t(gridDim.x) * kThreads)
-        ok = ok && isfinite(f.e[i]) && isfinite(f.h[i]);
+    for (uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x; i < quads; i += uint64_t(gridDim.x) * kThreads) {
+        const float4 a = __ldg(e + i), b = __ldg(h + i);
+        ok = ok && isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(a.w) && isfinite(b.x) &&
+             isfinite(b.y) && isfinite(b.z) && isfinite(b.w);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        for (uint64_t i = 4 * quads; i < total; ++i) ok = ok && isfinite(f.e[i]) && isfinite(f.h[i]);
     if (!__all_sync(0xffffffffu, ok) && (threadIdx.x & 31) == 0) atomicExch(flag, 0);
 }
 
@@ -276,8 +284,8 @@ void launch_energy_density(const DeviceScene &s, FieldSet f, float *dense_out, c
 }
 
 void launch_finite(const DeviceScene &s, FieldSet f, int32_t *flag, cudaStream_t stream) {
-    uint64_t b = blocks_for(3 * s.cells);
-    finite_pass<<<uint32_t(b < 2048 ? b : 2048), kThreads, 0, stream>>>(s, f, flag);
+    uint64_t b = blocks_for(3 * s.cells / 4 + 1);
+    finite_pass<<<uint32_t(b < 4864 ? b : 4864), kThreads, 0, stream>>>(s, f, flag);
 }
 
 } // namespace diaphane

@@ -13,41 +13,51 @@ namespace diaphane {
 
 namespace {
 
+// One block per row (blockIdx.y is the component), threads along the row: no
+// index division per element, and both sides of every row are contiguous.
 __global__ void pack_rows(const float *__restrict__ src, float *__restrict__ dst, uint32_t nx, uint32_t pitch,
-                          uint64_t rows, uint64_t src_stride, uint64_t total) {
-    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += uint64_t(gridDim.x) * blockDim.x) {
-        const uint64_t per = rows * nx;
-        const uint64_t c = i / per, r = (i % per) / nx, x = i % nx;
-        dst[i] = src[c * src_stride + r * pitch + x];
+                          uint64_t rows, uint64_t src_stride) {
+    const float *s = src + uint64_t(blockIdx.y) * src_stride;
+    float *d = dst + uint64_t(blockIdx.y) * rows * nx;
+    for (uint64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const float *sr = s + r * pitch;
+        float *dr = d + r * nx;
+        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) dr[x] = sr[x];
     }
 }
 
 __global__ void unpack_rows(const float *__restrict__ src, float *__restrict__ dst, uint32_t nx, uint32_t pitch,
-                            uint64_t rows, uint64_t dst_stride, uint64_t total) {
-    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += uint64_t(gridDim.x) * blockDim.x) {
-        const uint64_t per = rows * nx;
-        const uint64_t c = i / per, r = (i % per) / nx, x = i % nx;
-        dst[c * dst_stride + r * pitch + x] = src[i];
+                            uint64_t rows, uint64_t dst_stride) {
+    const float *s = src + uint64_t(blockIdx.y) * rows * nx;
+    float *d = dst + uint64_t(blockIdx.y) * dst_stride;
+    for (uint64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const float *sr = s + r * nx;
+        float *dr = d + r * pitch;
+        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) dr[x] = sr[x];
     }
 }
 
-unsigned blocks_for(uint64_t total) {
-    const uint64_t b = (total + 255) / 256;
-    return unsigned(b < 8192 ? (b ? b : 1) : 8192);
+dim3 row_grid(uint64_t rows, uint32_t components) {
+    return dim3(unsigned(rows < 16384 ? rows : 16384), components);
+}
+
+unsigned row_block(uint32_t nx) {
+    const uint32_t t = (nx + 31) / 32 * 32;
+    return t < 256 ? t : 256;
 }
 
 } // namespace
 
 void launch_pack_rows(const float *src, float *dst, uint32_t nx, uint32_t pitch, uint64_t rows, uint64_t src_stride,
                       uint32_t components, cudaStream_t stream) {
-    const uint64_t total = uint64_t(components) * rows * nx;
-    if (total) pack_rows<<<blocks_for(total), 256, 0, stream>>>(src, dst, nx, pitch, rows, src_stride, total);
+    if (uint64_t(components) * rows * nx == 0) return;
+    pack_rows<<<row_grid(rows, components), row_block(nx), 0, stream>>>(src, dst, nx, pitch, rows, src_stride);
 }
 
 void launch_unpack_rows(const float *src, float *dst, uint32_t nx, uint32_t pitch, uint64_t rows, uint64_t dst_stride,
                         uint32_t components, cudaStream_t stream) {
-    const uint64_t total = uint64_t(components) * rows * nx;
-    if (total) unpack_rows<<<blocks_for(total), 256, 0, stream>>>(src, dst, nx, pitch, rows, dst_stride, total);
+    if (uint64_t(components) * rows * nx == 0) return;
+    unpack_rows<<<row_grid(rows, components), row_block(nx), 0, stream>>>(src, dst, nx, pitch, rows, dst_stride);
 }
 
 namespace {

@@ -114,6 +114,21 @@ def test_energy_and_finiteness_match_the_oracle(threads):
     assert candidate.is_finite()
 
 
+@pytest.mark.parametrize("where", ["first", "middle", "last"])
+@pytest.mark.parametrize("value", [np.nan, np.inf, -np.inf])
+def test_a_single_non_finite_value_is_found(where, value):
+    scene, _ = scenes.materials()
+    sim = Simulation(scene)
+    sim.advance_by(10)
+    e = sim.read_electric()
+    e[{"first": 0, "middle": e.size // 2 + 1, "last": e.size - 1}[where]] = value
+    sim.write_electric(e)
+    assert not sim.is_finite()
+    e[np.isfinite(e) == False] = 0.0  # noqa: E712
+    sim.write_electric(e)
+    assert sim.is_finite()
+
+
 @pytest.mark.parametrize("z_chunk", [1, 5, 1000])
 def test_fused_chunking_does_not_change_a_bit(z_chunk, threads):
     """Every chunk boundary rebuilds new H one plane below itself; the planes
