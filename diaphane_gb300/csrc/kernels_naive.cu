@@ -7,6 +7,9 @@
 // fallback for scenes the fused kernel does not cover, an independent second
 // implementation the fused kernel is checked against, and the FP64 instance.
 #include "device.cuh"
+#include "exact_div.cuh"
+
+#include <stdexcept>
 
 namespace diaphane {
 
@@ -24,6 +27,34 @@ __device__ __forceinline__ bool decompose(uint64_t i, const DeviceScene &s, uint
     return c[0] < s.n[0];
 }
 
+// The cell of the H and E passes: block (row, x-chunk), thread along x; one
+// 32-bit division per thread.  False past nx.
+__device__ __forceinline__ bool cell_of(const DeviceScene &s, uint32_t c[3], uint64_t &i) {
+    c[0] = blockIdx.y * kThreads + threadIdx.x;
+    const uint32_t row = blockIdx.x;
+    c[1] = row % s.n[1];
+    c[2] = row / s.n[1];
+    i = uint64_t(row) * s.pitch + c[0];
+    return c[0] < s.n[0];
+}
+
+// ((1 -/+ loss) v -/+ g curl) / (1 +/- loss), the reference's semi-implicit
+// update: a lossless cell's is v -/+ g curl exactly (1 -/+ 0 = 1, x / 1 = x),
+// and an f32 lossy one divides without the library's slow path for tiny
+// numerators (exact_div).
+template <typename T> __device__ __forceinline__ T semi_implicit(T old, T loss, T drive) {
+    if (loss == T(0)) return old + drive;
+    const T n = (T(1) - loss) * old + drive;
+    if constexpr (sizeof(T) == 4) return exact_div(n, T(1) + loss);
+    else return n / (T(1) + loss);
+}
+// The inverse update (reversal runs only on lossless scenes, so the division
+// is not reached there; 1 - loss can be below 1, outside exact_div's range).
+template <typename T> __device__ __forceinline__ T semi_implicit_back(T old, T loss, T drive) {
+    if (loss == T(0)) return old + drive;
+    return ((T(1) + loss) * old + drive) / (T(1) - loss);
+}
+
 // Absorber sample: section 0 holds integer positions, section 1 half ones.
 __device__ __forceinline__ float profile(const float *absorber, uint32_t span, const uint32_t offset[3], int axis,
                                          uint32_t coord, bool half) {
@@ -38,10 +69,9 @@ __device__ __forceinline__ float profile(const float *absorber, uint32_t span, c
 template <typename T, bool Reverse>
 __global__ void __launch_bounds__(kThreads) magnetic_pass(DeviceScene s, const T *__restrict__ e,
                                                           T *__restrict__ h) {
-    const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
-    if (i >= s.cells) return;
     uint32_t c[3];
-    if (!decompose(i, s, c)) return;
+    uint64_t i;
+    if (!cell_of(s, c, i)) return;
     const uint64_t stride[3] = {1, s.pitch, uint64_t(s.pitch) * s.n[1]};
     const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
     const uint32_t span = s.n[0] + s.n[1] + s.n[2];
@@ -61,10 +91,8 @@ __global__ void __launch_bounds__(kThreads) magnetic_pass(DeviceScene s, const T
         const T loss = T((k.w + row) + profile(s.absorber, span, offset, 0, c[0], a != 0));
         T *target = h + uint64_t(a) * s.cells + i;
         const T old = *target;
-        if (Reverse)
-            *target = ((T(1) + loss) * old + T(k.z) * curl) / (T(1) - loss);
-        else
-            *target = ((T(1) - loss) * old - T(k.z) * curl) / (T(1) + loss);
+        if (Reverse) *target = semi_implicit_back(old, loss, T(k.z) * curl);
+        else *target = semi_implicit(old, loss, -(T(k.z) * curl));
     }
 }
 
@@ -73,10 +101,9 @@ __global__ void __launch_bounds__(kThreads) magnetic_pass(DeviceScene s, const T
 template <typename T, bool Reverse>
 __global__ void __launch_bounds__(kThreads) electric_pass(DeviceScene s, const T *__restrict__ h,
                                                           T *__restrict__ e) {
-    const uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x;
-    if (i >= s.cells) return;
     uint32_t c[3];
-    if (!decompose(i, s, c)) return;
+    uint64_t i;
+    if (!cell_of(s, c, i)) return;
     const uint64_t stride[3] = {1, s.pitch, uint64_t(s.pitch) * s.n[1]};
     const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
     const uint32_t span = s.n[0] + s.n[1] + s.n[2];
@@ -95,10 +122,8 @@ __global__ void __launch_bounds__(kThreads) electric_pass(DeviceScene s, const T
         const T loss = T((k.y + row) + profile(s.absorber, span, offset, 0, c[0], a == 0));
         T *target = e + uint64_t(a) * s.cells + i;
         const T old = *target;
-        if (Reverse)
-            *target = ((T(1) + loss) * old - T(k.x) * curl) / (T(1) - loss);
-        else
-            *target = ((T(1) - loss) * old + T(k.x) * curl) / (T(1) + loss);
+        if (Reverse) *target = semi_implicit_back(old, loss, -(T(k.x) * curl));
+        else *target = semi_implicit(old, loss, T(k.x) * curl);
     }
 }
 
@@ -215,18 +240,25 @@ uint32_t blocks_for(uint64_t n) { return uint32_t((n + kThreads - 1) / kThreads)
 
 namespace {
 
+// Blocks: one per (row, 256-cell chunk of the row).
+dim3 pass_grid(const DeviceScene &s) {
+    const uint64_t rows = uint64_t(s.n[1]) * s.n[2];
+    if (rows > 0x7fffffffull) throw std::runtime_error("grid has too many rows for the per-cell passes");
+    return dim3(unsigned(rows), (s.n[0] + kThreads - 1) / kThreads);
+}
+
 template <typename T> void magnetic(const DeviceScene &s, Fields<T> f, bool reverse, cudaStream_t stream) {
     if (reverse)
-        magnetic_pass<T, true><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.e, f.h);
+        magnetic_pass<T, true><<<pass_grid(s), kThreads, 0, stream>>>(s, f.e, f.h);
     else
-        magnetic_pass<T, false><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.e, f.h);
+        magnetic_pass<T, false><<<pass_grid(s), kThreads, 0, stream>>>(s, f.e, f.h);
 }
 
 template <typename T> void electric(const DeviceScene &s, Fields<T> f, bool reverse, cudaStream_t stream) {
     if (reverse)
-        electric_pass<T, true><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.h, f.e);
+        electric_pass<T, true><<<pass_grid(s), kThreads, 0, stream>>>(s, f.h, f.e);
     else
-        electric_pass<T, false><<<blocks_for(s.cells), kThreads, 0, stream>>>(s, f.h, f.e);
+        electric_pass<T, false><<<pass_grid(s), kThreads, 0, stream>>>(s, f.h, f.e);
 }
 
 template <typename T> void inject(const DeviceScene &s, Fields<T> f, const DeviceInjection &inj, T value,
