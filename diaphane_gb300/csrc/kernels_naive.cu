@@ -17,16 +17,6 @@ namespace {
 
 constexpr int kThreads = 256;
 
-// Cell coordinates of linear index i in a layout whose rows are `pitch`
-// cells long; false for the padding cells past nx.
-__device__ __forceinline__ bool decompose(uint64_t i, const DeviceScene &s, uint32_t c[3]) {
-    c[0] = uint32_t(i % s.pitch);
-    const uint64_t t = i / s.pitch;
-    c[1] = uint32_t(t % s.n[1]);
-    c[2] = uint32_t(t / s.n[1]);
-    return c[0] < s.n[0];
-}
-
 // The cell of the H and E passes: block (row, x-chunk), thread along x; one
 // 32-bit division per thread.  False past nx.
 __device__ __forceinline__ bool cell_of(const DeviceScene &s, uint32_t c[3], uint64_t &i) {
@@ -164,25 +154,45 @@ template <typename T>
 __global__ void __launch_bounds__(kThreads) energy_pass(DeviceScene s, Fields<T> f, const float *__restrict__ primary,
                                                         const float *__restrict__ dual,
                                                         const float2 *__restrict__ eps_mu, double *partials) {
-    const uint32_t offset[3] = {0, s.n[0], s.n[0] + s.n[1]};
+    // A component's volume is a product of one width per axis, so it splits
+    // into an x factor and a row (y, z) factor: E_x takes primary x, dual y
+    // and z; E_y and E_z dual x; H the other way round.  One warp per row sums
+    // x factor × energy in double along the row, and the row factors multiply
+    // once per row: a handful of double operations per cell instead of the
+    // three-way volume products (the device's f64 rate is what bounds this).
+    constexpr int kWarps = kThreads / 32;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t nx = s.n[0], ny = s.n[1], oy = s.n[0], oz = s.n[0] + s.n[1];
+    const uint64_t rows = uint64_t(ny) * s.n[2];
     double ee = 0.0, em = 0.0;
-    for (uint64_t i = uint64_t(blockIdx.x) * kThreads + threadIdx.x; i < s.cells;
-         i += uint64_t(gridDim.x) * kThreads) {
-        uint32_t c[3];
-        if (!decompose(i, s, c)) continue;
-        const float2 m = eps_mu[material_of(s, i)];
+    for (uint64_t row = uint64_t(blockIdx.x) * kWarps + warp; row < rows; row += uint64_t(gridDim.x) * kWarps) {
+        double sum[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        for (uint32_t x = lane; x < nx; x += 32) {
+            const uint64_t i = row * s.pitch + x;
+            const float2 m = eps_mu[material_of(s, i)];
+            const double px = double(__ldg(&primary[x])), dx = double(__ldg(&dual[x]));
+            double qe[3], qh[3];
 #pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            const int b = (a + 1) % 3, cc = (a + 2) % 3;
-            const T ev = f.e[uint64_t(a) * s.cells + i];
-            const T hv = f.h[uint64_t(a) * s.cells + i];
-            const double volume_e = double(primary[offset[a] + c[a]]) * double(dual[offset[b] + c[b]]) *
-                                    double(dual[offset[cc] + c[cc]]);
-            const double volume_h = double(dual[offset[a] + c[a]]) * double(primary[offset[b] + c[b]]) *
-                                    double(primary[offset[cc] + c[cc]]);
-            ee += 0.5 * volume_e * double(T(m.x) * ev * ev);
-            em += 0.5 * volume_h * double(T(m.y) * hv * hv);
+            for (int a = 0; a < 3; ++a) {
+                const T ev = f.e[uint64_t(a) * s.cells + i], hv = f.h[uint64_t(a) * s.cells + i];
+                qe[a] = double(T(m.x) * ev * ev);
+                qh[a] = double(T(m.y) * hv * hv);
+            }
+            // Fused multiply-adds in double (the build contracts nothing by
+            // itself): one rounding per term, well inside the 1e-9 the
+            // energy is checked to.
+            sum[0] = fma(px, qe[0], sum[0]);
+            sum[1] = fma(dx, qe[1], sum[1]);
+            sum[2] = fma(dx, qe[2], sum[2]);
+            sum[3] = fma(dx, qh[0], sum[3]);
+            sum[4] = fma(px, qh[1], sum[4]);
+            sum[5] = fma(px, qh[2], sum[5]);
         }
+        const uint32_t y = uint32_t(row % ny), z = uint32_t(row / ny);
+        const double py = double(primary[oy + y]), dy = double(dual[oy + y]);
+        const double pz = double(primary[oz + z]), dz = double(dual[oz + z]);
+        ee += 0.5 * ((dy * dz) * sum[0] + (py * dz) * sum[1] + (pz * dy) * sum[2]);
+        em += 0.5 * ((py * pz) * sum[3] + (dy * pz) * sum[4] + (dz * py) * sum[5]);
     }
     __shared__ double se[kThreads], sm[kThreads];
     se[threadIdx.x] = ee;

@@ -288,30 +288,45 @@ __global__ void volume_pass(ViewArgs v) {
 }
 
 // measure_peak: maxima over the real cells, by atomic max on the bit pattern
-// (ordered like the value for non-negative floats).
+// (ordered like the value for non-negative floats).  Blocks walk whole rows,
+// threads along them.  The averaged intensity's maximum is the maximum
+// intensity divided once: dividing by a positive count is monotonic under
+// round-to-nearest, so max(I / n) and max(I) / n are the same float.
 __global__ void measure_peak(const float *e, const float *h, const float *intensity, uint64_t stride, uint32_t nx,
                              uint32_t ny, uint32_t nz, uint32_t pitch, uint32_t accumulated, uint32_t *peak) {
     float local[kPeakSlots] = {0, 0, 0, 0, 0, 0, 0, 0};
-    const uint64_t cells = uint64_t(nx) * ny * nz;
-    for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < cells; i += uint64_t(gridDim.x) * blockDim.x) {
-        const uint32_t x = uint32_t(i % nx);
-        const uint64_t row = i / nx;
-        const uint64_t base = row * pitch + x;
-        float se = 0.0f, sh = 0.0f;
-        for (int c = 0; c < 3; ++c) {
-            const float ev = e[c * stride + base], hv = h[c * stride + base];
-            se += ev * ev;
-            sh += hv * hv;
-            local[1 + c] = fmaxf(local[1 + c], fabsf(ev));
-            local[4 + c] = fmaxf(local[4 + c], fabsf(hv));
+    float intensity_max = 0.0f;
+    const uint64_t rows = uint64_t(ny) * nz;
+    for (uint64_t row = blockIdx.x; row < rows; row += gridDim.x) {
+        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) {
+            const uint64_t base = row * pitch + x;
+            float se = 0.0f, sh = 0.0f;
+            for (int c = 0; c < 3; ++c) {
+                const float ev = e[c * stride + base], hv = h[c * stride + base];
+                se += ev * ev;
+                sh += hv * hv;
+                local[1 + c] = fmaxf(local[1 + c], fabsf(ev));
+                local[4 + c] = fmaxf(local[4 + c], fabsf(hv));
+            }
+            local[0] = fmaxf(local[0], fmaxf(0.5f * se, 0.5f * sh));
+            intensity_max = fmaxf(intensity_max, intensity[base]);
         }
-        local[0] = fmaxf(local[0], fmaxf(0.5f * se, 0.5f * sh));
-        local[7] = fmaxf(local[7], intensity[base] / float(max(accumulated, 1u)));
     }
+    local[7] = intensity_max / float(max(accumulated, 1u));
+    // Warp maxima, then block maxima in shared memory: one atomic per slot
+    // per block (all blocks' atomics land on the same eight words).
+    __shared__ float warp_max[kPeakSlots][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
     for (int s = 0; s < kPeakSlots; ++s) {
         float m = local[s];
         for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-        if ((threadIdx.x & 31) == 0) atomicMax(peak + s, __float_as_uint(m));
+        if (lane == 0) warp_max[s][warp] = m;
+    }
+    __syncthreads();
+    if (threadIdx.x < kPeakSlots) {
+        float m = 0.0f;
+        for (int w = 0; w < warps; ++w) m = fmaxf(m, warp_max[threadIdx.x][w]);
+        atomicMax(peak + threadIdx.x, __float_as_uint(m));
     }
 }
 
@@ -346,7 +361,7 @@ struct dp_renderer {
         check_cuda(cudaMemsetAsync(peak, 0, kPeakSlots * sizeof(uint32_t), sim->stream), "clear peak");
         const FieldSet f = sim->fields();
         const uint32_t accumulated = uint32_t(std::min<uint64_t>(sim->accumulated, 0xffffffffu));
-        measure_peak<<<1024, 256, 0, sim->stream>>>(f.e, f.h, sim->intensity, sim->padded_cells(), n[0], n[1], n[2],
+        measure_peak<<<2048, 256, 0, sim->stream>>>(f.e, f.h, sim->intensity, sim->padded_cells(), n[0], n[1], n[2],
                                                     sim->pitch, accumulated, peak);
         check_cuda(cudaGetLastError(), "measure peak");
         check_cuda(cudaMemcpyAsync(peak_host, peak, kPeakSlots * sizeof(uint32_t), cudaMemcpyDeviceToHost, sim->stream),
