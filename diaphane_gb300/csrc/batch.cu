@@ -125,6 +125,7 @@ struct Entry {
     std::vector<uint32_t> probe_cells; // padded linear cell index per probe
     float *probes = nullptr;      // target × probes × 2 (Ez, Hy)
     std::vector<BatchUnit> units;
+    IncidentLines<float> lines;   // the scene's total-field boxes, if any
 };
 
 // Per-step probe gather: after step t of a chunk, Ez and Hy at every probe
@@ -190,6 +191,11 @@ struct dp_batch {
     BatchScene *h_scenes[2] = {nullptr, nullptr};
     DeviceInjection *h_injections[2] = {nullptr, nullptr};
     uint32_t *h_counts[2] = {nullptr, nullptr};
+    // Total-field boxes' side-face values of one chunk, per staging half:
+    // every box scene's steps back to back, indexed by its injections.
+    float *profiles = nullptr;                    // [2][profile_capacity] device
+    float *h_profiles[2] = {nullptr, nullptr};    // pinned
+    size_t profile_capacity = 0;
     cudaEvent_t staged[2] = {nullptr, nullptr};
     int stage = 0;
     // Graph of one chunk, rebuilt when the work lists change.
@@ -217,7 +223,9 @@ struct dp_batch {
         for (cudaEvent_t e : joins) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
         cudaFree(arena_base);
+        cudaFree(profiles);
         for (int k = 0; k < 2; ++k) {
+            cudaFreeHost(h_profiles[k]);
             cudaFreeHost(h_scenes[k]);
             cudaFreeHost(h_injections[k]);
             cudaFreeHost(h_counts[k]);
@@ -253,6 +261,22 @@ struct dp_batch {
             if (deep_units >= 16ull * uint64_t(sm_count)) depth = 64;
         }
         for (auto &kv : entries) make_units(kv.second, depth);
+        // Room for a whole chunk of every box scene's side-face values (the
+        // stream is idle here, so the old buffers can go).
+        size_t profile_need = 0;
+        for (auto &kv : entries) profile_need += size_t(chunk) * kv.second.lines.profile_width();
+        if (profile_need > profile_capacity) {
+            cudaFree(profiles);
+            profiles = nullptr;
+            for (auto &hp : h_profiles) {
+                cudaFreeHost(hp);
+                hp = nullptr;
+            }
+            profile_capacity = 0;
+            check(cudaMalloc(&profiles, 2 * profile_need * sizeof(float)), "cudaMalloc profiles");
+            for (auto &hp : h_profiles) check(cudaMallocHost(&hp, profile_need * sizeof(float)), "profile staging");
+            profile_capacity = profile_need;
+        }
         std::vector<std::vector<BatchUnit>> lists;
         std::vector<std::vector<ProbeSlot>> probe_lists;
         for (auto &kv : entries) {
@@ -317,13 +341,14 @@ struct dp_batch {
     void record_chunk(int half) {
         const DeviceInjection *inj = injections + size_t(half) * injection_span();
         const uint32_t *cnt = counts + size_t(half) * count_span();
+        const float *prof = profiles ? profiles + size_t(half) * profile_capacity : nullptr;
         check(cudaEventRecord(fork, stream), "fork");
         for (size_t v = 0; v < variants.size(); ++v) {
             cudaStream_t lane = lanes[v];
             check(cudaStreamWaitEvent(lane, fork, 0), "fork");
             for (uint32_t t = 0; t < chunk; ++t) {
                 launch_batch_step(variants[v].cx, variants[v].tile_y, variants[v].slots, scenes, units[v],
-                                  unit_counts[v], inj, cnt, capacity, t, error, lane);
+                                  unit_counts[v], inj, cnt, prof, capacity, t, error, lane);
                 ++launches;
                 if (probe_count_v[v]) {
                     gather_probes<<<(probe_count_v[v] + 255) / 256, 256, 0, lane>>>(
@@ -352,6 +377,9 @@ struct dp_batch {
         std::memset(hc, 0, count_span() * sizeof(uint32_t));
         uint32_t stepping = 0;
         std::vector<StepInjection> step_injections;
+        std::vector<float> step_profiles;
+        size_t profile_cursor = 0;
+        float *hp = h_profiles[half];
         std::vector<ProbeSlot> probe_updates;
         for (auto &kv : entries) {
             Entry &e = kv.second;
@@ -364,7 +392,17 @@ struct dp_batch {
             if (steps) ++stepping;
             for (uint32_t t = 0; t < steps; ++t) {
                 const float time = float(e.step + t + 1) * e.scene.dt;
-                e.scene.injections(time, step_injections);
+                int32_t rebase = 0;
+                if (e.lines.empty()) {
+                    e.scene.injections(time, step_injections);
+                } else {
+                    e.scene.injections_in<float>(time, step_injections, &e.lines.at(e.step + t), &step_profiles);
+                    if (profile_cursor + step_profiles.size() > profile_capacity)
+                        throw Error(DP_ERR_CUDA, "box profiles exceed the batch's staging");
+                    std::memcpy(hp + profile_cursor, step_profiles.data(), step_profiles.size() * sizeof(float));
+                    rebase = int32_t(profile_cursor);
+                    profile_cursor += step_profiles.size();
+                }
                 uint32_t n = 0;
                 DeviceInjection *row = hi + (size_t(t) * capacity + e.slot) * kBatchInjections;
                 for (const StepInjection &si : step_injections) {
@@ -379,8 +417,8 @@ struct dp_batch {
                     d.magnetic = si.magnetic;
                     d.value = si.value;
                     d.weight_offset = si.weight_offset;
-                    d.profile_offset = -1; // a batch scene has no total-field box
-                    d.profile_axis = 0;
+                    d.profile_offset = si.profile_offset < 0 ? -1 : si.profile_offset + rebase;
+                    d.profile_axis = si.profile_axis;
                 }
                 hc[size_t(t) * capacity + e.slot] = n;
             }
@@ -393,6 +431,10 @@ struct dp_batch {
         check(cudaMemcpyAsync(counts + size_t(half) * count_span(), hc, count_span() * sizeof(uint32_t),
                               cudaMemcpyHostToDevice, stream),
               "counts");
+        if (profile_cursor)
+            check(cudaMemcpyAsync(profiles + size_t(half) * profile_capacity, hp, profile_cursor * sizeof(float),
+                                  cudaMemcpyHostToDevice, stream),
+                  "profiles");
         check(cudaEventRecord(staged[half], stream), "staging event");
         if (stepping) {
             if (graphs && !changed) {
@@ -543,12 +585,10 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         if (!b || !scene || !id || (probe_count && !probes)) throw Error(DP_ERR_INVALID, "null argument");
         const Scene &s = scene_of(scene);
         if (!tensor_maps_available()) throw Error(DP_ERR_UNSUPPORTED, "the CUDA driver offers no tensor-map encoder");
-        if (2 * s.sources.size() > size_t(kBatchInjections))
-            throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 4 sources");
+        if (s.injection_slots() > size_t(kBatchInjections))
+            throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 8 injection slots (2 per source, 8 for a "
+                                            "total-field box)");
         if (s.index_bytes != 1) throw Error(DP_ERR_UNSUPPORTED, "a batch scene carries at most 256 materials");
-        if (s.has_boxes())
-            throw Error(DP_ERR_UNSUPPORTED, "a batch scene takes no total-field box (its side faces need per-step "
-                                            "profiles the batch does not stage)");
         uint32_t slot = 0;
         while (slot < b->capacity && b->slot_used[slot]) ++slot;
         if (slot == b->capacity) throw Error(DP_ERR_BUSY, "every scene slot of the batch is in use");
@@ -559,6 +599,7 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         Entry e;
         e.id = b->next_id++;
         e.scene = s;
+        e.lines = IncidentLines<float>(s);
         e.slot = slot;
         e.variant = variant_for(s.grid.n[0], b->cells_per_lane);
         e.pitch = l.pitch;

@@ -174,10 +174,12 @@ struct BatchUnit {
 void batch_scene_maps(BatchScene &scene, uint32_t cx, uint32_t tile_y, const uint8_t *material,
                       uint32_t material_pitch);
 // One launch per step over every unit of one kernel variant.
+// `profiles`: the chunk's total-field box profile values (device), which the
+// injections' profile offsets index; null when no scene of the batch has a box.
 void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, const BatchScene *scenes,
                        const BatchUnit *units, uint32_t unit_count, const DeviceInjection *injections,
-                       const uint32_t *injection_counts, uint32_t scene_count, uint32_t step, int32_t *error,
-                       cudaStream_t stream);
+                       const uint32_t *injection_counts, const float *profiles, uint32_t scene_count,
+                       uint32_t step, int32_t *error, cudaStream_t stream);
 size_t fused_variant_smem(uint32_t cx, uint32_t tile_y, uint32_t slots);
 // Sets every batch kernel's shared-memory attributes (before any capture).
 void configure_batch_kernels();

@@ -830,7 +830,7 @@ template <int CX, int TY, int SLOTS>
 __global__ void __launch_bounds__(32 * TY, resident_ctas(CX, TY, SLOTS))
 fused_batch_step(const BatchScene *__restrict__ scenes, const BatchUnit *__restrict__ units,
                  const DeviceInjection *__restrict__ injections, const uint32_t *__restrict__ injection_counts,
-                 uint32_t scene_count, uint32_t step, int32_t *error) {
+                 const float *__restrict__ profiles, uint32_t scene_count, uint32_t step, int32_t *error) {
     const BatchUnit unit = units[blockIdx.x];
     const BatchScene &bs = scenes[unit.scene];
     if (step >= bs.steps) return;
@@ -851,7 +851,7 @@ fused_batch_step(const BatchScene *__restrict__ scenes, const BatchUnit *__restr
     u.intensity = bs.intensity;
     u.error = error;
     const size_t slot = size_t(step) * scene_count + unit.scene;
-    u.inj = InjectionView{injections + slot * kBatchInjections, injection_counts[slot], nullptr};
+    u.inj = InjectionView{injections + slot * kBatchInjections, injection_counts[slot], profiles};
     u.x0 = int(unit.x0);
     u.y0 = int(unit.y0);
     u.z0 = int(unit.z0);
@@ -1040,10 +1040,10 @@ template <int CX, int TY, int SLOTS> void configure_batch_variant() {
 
 template <int CX, int TY, int SLOTS>
 void launch_batch_variant(const BatchScene *scenes, const BatchUnit *units, uint32_t unit_count,
-                          const DeviceInjection *injections, const uint32_t *counts, uint32_t scene_count,
-                          uint32_t step, int32_t *error, cudaStream_t stream) {
+                          const DeviceInjection *injections, const uint32_t *counts, const float *profiles,
+                          uint32_t scene_count, uint32_t step, int32_t *error, cudaStream_t stream) {
     fused_batch_step<CX, TY, SLOTS><<<unit_count, 32 * TY, Geometry<CX, TY, SLOTS>::SMEM, stream>>>(
-        scenes, units, injections, counts, scene_count, step, error);
+        scenes, units, injections, counts, profiles, scene_count, step, error);
 }
 
 } // namespace
@@ -1058,15 +1058,15 @@ bool tensor_maps_available() { return encoder() != nullptr; }
 
 void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, const BatchScene *scenes,
                        const BatchUnit *units, uint32_t unit_count, const DeviceInjection *injections,
-                       const uint32_t *injection_counts, uint32_t scene_count, uint32_t step, int32_t *error,
-                       cudaStream_t stream) {
+                       const uint32_t *injection_counts, const float *profiles, uint32_t scene_count,
+                       uint32_t step, int32_t *error, cudaStream_t stream) {
     if (unit_count == 0) return;
     if (cx == 4 && tile_y == 8 && slots == 3)
-        launch_batch_variant<4, 8, 3>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
+        launch_batch_variant<4, 8, 3>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
     else if (cx == 2 && tile_y == 8 && slots == 3)
-        launch_batch_variant<2, 8, 3>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
+        launch_batch_variant<2, 8, 3>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
     else if (cx == 1 && tile_y == 8 && slots == 4)
-        launch_batch_variant<1, 8, 4>(scenes, units, unit_count, injections, injection_counts, scene_count, step, error, stream);
+        launch_batch_variant<1, 8, 4>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
     else
         throw std::runtime_error("no batch kernel variant with that tile shape and ring depth");
 }

@@ -123,8 +123,8 @@ enum { DP_SOURCE_POINT = 0, DP_SOURCE_SHEET = 1, DP_SOURCE_PLANE_WAVE = 2, DP_SO
  * total-field box, with the scattered field alone outside the box on every
  * side.  Its incident field is a 1-D Yee line along the travel axis stepped
  * with the grid's own gains, driven by the plane-wave corrections of
- * src/source.rs:334-401; the box faces must lie in vacuum.  The batch and
- * time reversal refuse it (DP_ERR_UNSUPPORTED). */
+ * src/source.rs:334-401; the box faces must lie in vacuum.  Time reversal
+ * refuses it (DP_ERR_UNSUPPORTED: the line absorbs at its far end). */
 typedef struct dp_source {
     uint32_t shape;
     uint32_t polarization; /* driven E component */

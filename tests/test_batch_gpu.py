@@ -60,7 +60,6 @@ def test_scenes_that_join_and_leave_between_chunks(threads):
 
 def test_the_parity_scenes_in_one_batch(threads):
     cases = {name: make() for name, make in scenes.PARITY_CASES.items()}
-    cases = {name: case for name, case in cases.items() if not scenes.has_box(case[0])}
     batch = Batch(ARENA, chunk_steps=50, max_scenes=16)
     ids = {name: batch.add(ResolvedScene(scene), steps) for name, (scene, steps) in cases.items()}
     batch.run_to_completion()
@@ -123,10 +122,26 @@ def test_reads_into_a_caller_buffer_match_fresh_arrays():
             assert np.array_equal(bits(read_solo(out=pinned)), bits(fresh))
 
 
-def test_a_total_field_box_is_refused_by_the_batch():
-    from diaphane_gb300 import _abi
+def test_a_total_field_box_in_a_batch_matches_its_solo_run(threads):
+    # The box's side faces read per-step profiles the batch stages per chunk;
+    # mixed with other scenes and split over several chunks, it must still
+    # come out bit-identical to its solo run and to the oracle.
     scene, steps = scenes.box_wave()
-    batch = Batch(ARENA, chunk_steps=16, max_scenes=4)
-    with pytest.raises(Exception) as failure:
-        batch.add(ResolvedScene(scene), steps)
-    assert failure.value.status == _abi.DP_ERR_UNSUPPORTED
+    others = mixed(3, steps, seed0=4000)
+    batch = Batch(ARENA, chunk_steps=32, max_scenes=8)
+    box = batch.add(ResolvedScene(scene), steps, accumulate_intensity=True)
+    ids = [batch.add(r, steps - 11 * k) for k, r in enumerate(others)]
+    batch.run_to_completion()
+    solo = Simulation(scene)
+    solo.set_accumulate_intensity(True)
+    solo.advance_by(steps)
+    assert np.array_equal(bits(batch.read_electric(box)), bits(solo.read_electric()))
+    assert np.array_equal(bits(batch.read_magnetic(box)), bits(solo.read_magnetic()))
+    assert np.array_equal(bits(batch.read_intensity(box)), bits(solo.read_intensity()))
+    ref = oracle.OracleSimulation(scene, threads=threads)
+    ref.advance_by(steps)
+    assert np.array_equal(bits(batch.read_electric(box)), bits(ref.read_electric()))
+    for k, (ident, r) in enumerate(zip(ids, others)):
+        alone = Simulation(r)
+        alone.advance_by(steps - 11 * k)
+        assert np.array_equal(bits(batch.read_electric(ident)), bits(alone.read_electric())), k
