@@ -88,7 +88,7 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
                                         "total-field box) and 256 materials (and needs the tensor-map encoder)");
     sim->kernel = (requested == DP_KERNEL_NAIVE || !fits) ? DP_KERNEL_NAIVE : DP_KERNEL_FUSED;
     sim->lines = IncidentLines<float>(s);
-    if (sim->lines.profile_width()) sim->profile_ring.create(sim->lines.profile_width(), 64);
+    if (sim->lines.profile_width()) sim->profile_ring.create(sim->lines.profile_width(), 256);
 
     DeviceScene &d = sim->dev;
     for (int a = 0; a < 3; ++a) d.n[a] = s.grid.n[a];

@@ -142,7 +142,7 @@ dp_status dp_sim64_create(const dp_scene *scene, int32_t device, dp_sim64 **out)
         check(cudaStreamCreateWithFlags(&sim->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         const Scene &s = sim->scene;
         sim->lines = IncidentLines<double>(s);
-        if (sim->lines.profile_width()) sim->profile_ring.create(sim->lines.profile_width(), 64);
+        if (sim->lines.profile_width()) sim->profile_ring.create(sim->lines.profile_width(), 256);
         const uint64_t cells = s.grid.cells();
         DeviceScene &d = sim->dev;
         for (int a = 0; a < 3; ++a) d.n[a] = s.grid.n[a];
