@@ -303,15 +303,20 @@ __device__ __forceinline__ void apply_injections(const InjectionView &t, const f
             // Weight 1 everywhere (a point, a plane, a box's uniform face):
             // value * 1 is value, so each covered cell just adds it.
             const int dx0 = x - int(d.origin[0]);
-            const uint32_t ex = d.extent[0], c = d.component;
+            const uint32_t ex = d.extent[0];
             const float add = d.value;
+            // The component is the injection's, the same on every lane: one
+            // branch, then selects (not an added zero: -0 + 0 would turn a
+            // cell's -0 into +0).
+            if (d.component == 0) {
 #pragma unroll
-            for (int j = 0; j < CX; ++j) {
-                // Selects, not an added zero: -0 + 0 would turn a cell's -0 into +0.
-                const bool in = uint32_t(dx0 + j) < ex;
-                f0.v[j] = (in && c == 0) ? f0.v[j] + add : f0.v[j];
-                f1.v[j] = (in && c == 1) ? f1.v[j] + add : f1.v[j];
-                f2.v[j] = (in && c == 2) ? f2.v[j] + add : f2.v[j];
+                for (int j = 0; j < CX; ++j) f0.v[j] = uint32_t(dx0 + j) < ex ? f0.v[j] + add : f0.v[j];
+            } else if (d.component == 1) {
+#pragma unroll
+                for (int j = 0; j < CX; ++j) f1.v[j] = uint32_t(dx0 + j) < ex ? f1.v[j] + add : f1.v[j];
+            } else {
+#pragma unroll
+                for (int j = 0; j < CX; ++j) f2.v[j] = uint32_t(dx0 + j) < ex ? f2.v[j] + add : f2.v[j];
             }
             continue;
         }
@@ -447,8 +452,16 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
     // the grid) are computed but never stored.
     const int full_lane = nx - xl >= CX ? CX : nx - xl;
     const bool has_inj = inj.count != 0;
-    const uint32_t mask_h = has_inj ? injection_mask(inj, true, xl, xl + CX, y, zs, z1) : 0u;
-    const uint32_t mask_e = has_inj ? injection_mask(inj, false, xl, xl + CX, y, zs, z1) : 0u;
+    // Both phases' masks in one pass over the table.
+    uint32_t mask_h = 0, mask_e = 0;
+    for (uint32_t k = 0; k < inj.count; ++k) {
+        const DeviceInjection &d = inj.item[k];
+        if (y >= int(d.origin[1]) && y < int(d.origin[1] + d.extent[1]) && xl + CX > int(d.origin[0]) &&
+            xl < int(d.origin[0] + d.extent[0]) && z1 > int(d.origin[2]) && zs < int(d.origin[2] + d.extent[2])) {
+            if (d.magnetic) mask_h |= 1u << k;
+            else mask_e |= 1u << k;
+        }
+    }
 
     // Halo cells, packed onto the first warps: halo index i = 32·warp + lane;
     // i < TX takes cell x0+i of row y0-1 (the Hx, Hz that E at row y0 reads),
