@@ -13,16 +13,25 @@ namespace diaphane {
 
 namespace {
 
-// One block per row (blockIdx.y is the component), threads along the row: no
-// index division per element, and both sides of every row are contiguous.
+// Blocks walk groups of four rows (blockIdx.y is the component), threads
+// along them; the four loads of a thread are issued before its stores, so a
+// thread keeps four requests in flight.  No index division per element.
+constexpr uint32_t kRowsPerStep = 4;
+
 __global__ void pack_rows(const float *__restrict__ src, float *__restrict__ dst, uint32_t nx, uint32_t pitch,
                           uint64_t rows, uint64_t src_stride) {
     const float *s = src + uint64_t(blockIdx.y) * src_stride;
     float *d = dst + uint64_t(blockIdx.y) * rows * nx;
-    for (uint64_t r = blockIdx.x; r < rows; r += gridDim.x) {
-        const float *sr = s + r * pitch;
-        float *dr = d + r * nx;
-        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) dr[x] = sr[x];
+    for (uint64_t r0 = uint64_t(blockIdx.x) * kRowsPerStep; r0 < rows; r0 += uint64_t(gridDim.x) * kRowsPerStep) {
+        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) {
+            float v[kRowsPerStep];
+#pragma unroll
+            for (uint32_t k = 0; k < kRowsPerStep; ++k)
+                if (r0 + k < rows) v[k] = s[(r0 + k) * pitch + x];
+#pragma unroll
+            for (uint32_t k = 0; k < kRowsPerStep; ++k)
+                if (r0 + k < rows) d[(r0 + k) * nx + x] = v[k];
+        }
     }
 }
 
@@ -30,15 +39,22 @@ __global__ void unpack_rows(const float *__restrict__ src, float *__restrict__ d
                             uint64_t rows, uint64_t dst_stride) {
     const float *s = src + uint64_t(blockIdx.y) * rows * nx;
     float *d = dst + uint64_t(blockIdx.y) * dst_stride;
-    for (uint64_t r = blockIdx.x; r < rows; r += gridDim.x) {
-        const float *sr = s + r * nx;
-        float *dr = d + r * pitch;
-        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) dr[x] = sr[x];
+    for (uint64_t r0 = uint64_t(blockIdx.x) * kRowsPerStep; r0 < rows; r0 += uint64_t(gridDim.x) * kRowsPerStep) {
+        for (uint32_t x = threadIdx.x; x < nx; x += blockDim.x) {
+            float v[kRowsPerStep];
+#pragma unroll
+            for (uint32_t k = 0; k < kRowsPerStep; ++k)
+                if (r0 + k < rows) v[k] = s[(r0 + k) * nx + x];
+#pragma unroll
+            for (uint32_t k = 0; k < kRowsPerStep; ++k)
+                if (r0 + k < rows) d[(r0 + k) * pitch + x] = v[k];
+        }
     }
 }
 
 dim3 row_grid(uint64_t rows, uint32_t components) {
-    return dim3(unsigned(rows < 16384 ? rows : 16384), components);
+    const uint64_t groups = (rows + kRowsPerStep - 1) / kRowsPerStep;
+    return dim3(unsigned(groups < 16384 ? groups : 16384), components);
 }
 
 unsigned row_block(uint32_t nx) {
