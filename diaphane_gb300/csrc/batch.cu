@@ -15,6 +15,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <thread>
@@ -50,6 +51,7 @@ class Arena {
         capacity_ = capacity;
     }
     bool allocate(size_t bytes, size_t &offset) {
+        if (bytes > SIZE_MAX - kAlign) return false;
         bytes = round_up(bytes, kAlign);
         for (auto it = free_.begin(); it != free_.end(); ++it) {
             if (it->second >= bytes) {
@@ -495,8 +497,17 @@ struct Layout {
     size_t fields, intensity, material, coeff, gains, absorber, weights, probes, total;
 };
 
+// Probe series longer than this many values (4 TiB) fit no arena; the
+// layout of such a scene reports SIZE_MAX bytes instead of a wrapped product.
+constexpr uint64_t kMaxProbeValues = uint64_t(1) << 40;
+
 Layout layout_of(const Scene &s, uint32_t probe_count, uint64_t steps) {
     Layout l{};
+    const uint64_t probe_values = uint64_t(probe_count) * 2;
+    if (probe_values && steps > kMaxProbeValues / probe_values) {
+        l.total = SIZE_MAX;
+        return l;
+    }
     const uint32_t *n = s.grid.n;
     l.pitch = (n[0] + 3) / 4 * 4;
     l.material_pitch = (n[0] + 15) / 16 * 16;
@@ -593,6 +604,7 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         while (slot < b->capacity && b->slot_used[slot]) ++slot;
         if (slot == b->capacity) throw Error(DP_ERR_BUSY, "every scene slot of the batch is in use");
         const Layout l = layout_of(s, probe_count, steps);
+        if (l.total == SIZE_MAX) throw Error(DP_ERR_OOM, "the probe series of this many steps fit no arena");
         size_t offset = 0;
         if (!b->arena.allocate(l.total, offset)) throw Error(DP_ERR_OOM, "the batch arena cannot hold this scene now");
         b->bind();

@@ -422,6 +422,9 @@ dp_status dp_sim_set_probes(dp_sim *sim, const uint32_t *cells, uint32_t count, 
     return guarded([&] {
         if (!sim || (count && !cells)) throw Error(DP_ERR_INVALID, "null argument");
         if (count && capacity == 0) throw Error(DP_ERR_INVALID, "a probe ring needs room for at least one step");
+        // Checked before the byte count is formed, so it cannot wrap.
+        if (count && capacity > (uint64_t(1) << 40) / (uint64_t(count) * 2))
+            throw Error(DP_ERR_OOM, "a probe ring of more than 2^40 values");
         const uint32_t *n = sim->scene.grid.n;
         std::vector<uint32_t> padded(count);
         for (uint32_t k = 0; k < count; ++k) {

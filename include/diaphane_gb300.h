@@ -356,7 +356,9 @@ dp_status dp_batch_read_field(dp_batch *batch, uint64_t id, uint32_t field, floa
 /* Probe series: step-major, then probe, then (Ez, Hy). */
 dp_status dp_batch_read_probes(dp_batch *batch, uint64_t id, float *host, size_t count);
 dp_status dp_batch_memory(const dp_batch *batch, uint64_t *used, uint64_t *capacity);
-/* Arena bytes a scene would take (for admission control). */
+/* Arena bytes a scene would take (for admission control); UINT64_MAX when
+ * its probe series (probe_count x steps x 2 values) would exceed 2^40 values,
+ * which no arena holds (dp_batch_add then returns DP_ERR_OOM). */
 uint64_t dp_scene_batch_bytes(const dp_scene *scene, uint32_t probe_count, uint64_t steps);
 uint64_t dp_batch_launch_count(const dp_batch *batch);
 
@@ -401,7 +403,9 @@ dp_status dp_sim_autotune(dp_sim *sim, uint32_t steps, dp_tuning *out);
  * Probes record Ez and Hy at given cells after every step into a device ring
  * of `capacity` steps (one small gather launch per step while set); count 0
  * removes them.  A restore, reset or field write starts a new history, and
- * only steps recorded since are readable. */
+ * only steps recorded since are readable.  A ring of more than 2^40 values
+ * (capacity x count x 2) is refused with DP_ERR_OOM before anything is
+ * allocated. */
 dp_status dp_sim_set_probes(dp_sim *sim, const uint32_t *cells_xyz, uint32_t count, uint64_t capacity);
 /* Steps first_step .. first_step+steps-1 (step k = the state after k steps),
  * steps × probes × (Ez, Hy) floats; DP_ERR_RANGE outside the ring. */

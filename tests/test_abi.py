@@ -51,3 +51,18 @@ def test_read_buffers_are_checked_before_any_copy():
     for bad in [np.zeros(5, dtype=np.float64), np.zeros(4, dtype=np.float32), np.zeros((4, 4), np.float32)[:, 0]]:
         with pytest.raises(ValueError):
             _output(bad, 5)
+
+
+def test_batch_bytes_saturate_instead_of_wrapping():
+    """A probe series of probe_count x steps x 2 values is sized with an
+    overflow check: past 2^40 values the scene's arena size reads UINT64_MAX
+    (and dp_batch_add refuses it) rather than a wrapped small number.
+    Host-only: no device call."""
+    from diaphane_gb300 import Batch, Extent, ResolvedScene, Scene
+    resolved = ResolvedScene(Scene.photon(Extent.cube(32)))
+    plain = Batch.bytes_for(resolved, 100)
+    assert 0 < plain < 1 << 30
+    assert Batch.bytes_for(resolved, 100, probe_count=8) > plain
+    assert Batch.bytes_for(resolved, 1 << 62, probe_count=8) == (1 << 64) - 1
+    assert Batch.bytes_for(resolved, (1 << 40) // 16, probe_count=8) < 1 << 45
+    assert Batch.bytes_for(resolved, 1 << 62, probe_count=0) < 1 << 30

@@ -99,6 +99,17 @@ def test_admission_refuses_what_the_arena_cannot_hold():
     with pytest.raises(DiaphaneError) as err:
         batch.add(r, 100)
     assert err.value.name == "DP_ERR_OOM"
+    # A probe series whose size would wrap is refused as unfittable, not
+    # admitted at a wrapped small size; the batch carries on.
+    big = Batch(int(need * 2.5), chunk_steps=10, max_scenes=8)
+    with pytest.raises(DiaphaneError) as err:
+        big.add(r, 1 << 62, probes=[(1, 1, 1)])
+    assert err.value.name == "DP_ERR_OOM"
+    ident = big.add(r, 20)
+    big.run_to_completion()
+    solo = Simulation(r)
+    solo.advance_by(20)
+    assert np.array_equal(bits(big.read_electric(ident)), bits(solo.read_electric()))
 
 
 def test_reads_into_a_caller_buffer_match_fresh_arrays():

@@ -119,6 +119,13 @@ def test_probes_record_every_step_like_the_oracle(threads):
     assert np.array_equal(bits(sim.read_probes(1, 3)), bits(expected[0:3]))
     with pytest.raises(DiaphaneError):
         sim.set_probes([(n[0], 0, 0)], 8)
+    # A ring whose byte count would wrap is refused before anything changes:
+    # the current probes keep recording.
+    with pytest.raises(DiaphaneError) as err:
+        sim.set_probes(cells, 1 << 62)
+    assert err.value.status == _abi.DP_ERR_OOM
+    sim.advance_by(2)
+    assert np.array_equal(bits(sim.read_probes(4, 2)), bits(expected[3:5]))
 
 
 def test_asynchronous_read_matches_the_synchronous_one():
