@@ -124,6 +124,8 @@ dp_status dp_keyframes_create(dp_sim *sim, uint64_t interval, uint32_t capacity,
         k->interval = interval;
         k->capacity = capacity;
         k->slot_floats = 6 * sim->padded_cells();
+        if (capacity > SIZE_MAX / sizeof(float) / k->slot_floats)
+            throw Error(DP_ERR_OOM, "a keyframe store larger than the address space");
         sim->bind();
         check_cuda(cudaMalloc(&k->store, size_t(capacity) * k->slot_floats * sizeof(float)), "keyframe store");
         for (uint32_t s = capacity; s-- > 0;) k->free_slots.push_back(s);
