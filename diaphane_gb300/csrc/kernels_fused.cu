@@ -41,6 +41,7 @@
 
 #include <cuda.h>
 
+#include <atomic>
 #include <cstdio>
 #include <stdexcept>
 #include <string>
@@ -902,13 +903,19 @@ void encode(CUtensorMap *map, CUtensorMapDataType type, int rank, void *base, co
     if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed: " + std::to_string(int(r)));
 }
 
+// A kernel's shared-memory opt-in is an attribute of the current device's
+// context, so it is set once per device (a bit per device ordinal; host
+// threads may race to set it, which is harmless).
 template <int CX, int TY, int SLOTS> void configure() {
-    static bool done = false;
-    if (done) return;
+    static std::atomic<uint64_t> done{0};
+    int device = 0;
+    cudaGetDevice(&device);
+    const uint64_t bit = device < 64 ? uint64_t(1) << device : 0;
+    if (bit && (done.load(std::memory_order_acquire) & bit)) return;
     cudaFuncSetAttribute(fused_step<CX, TY, SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          Geometry<CX, TY, SLOTS>::SMEM);
     cudaFuncSetAttribute(fused_step<CX, TY, SLOTS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-    done = true;
+    done.fetch_or(bit, std::memory_order_release);
 }
 
 template <int CX, int TY, int SLOTS> size_t smem_of() { return Geometry<CX, TY, SLOTS>::SMEM; }
