@@ -102,7 +102,12 @@ class Server:
             queue.popleft()
 
     def _finished(self, active: dict) -> list:
-        return [ident for ident in active if self.batch.status(ident)[0] >= self.batch.status(ident)[1]]
+        done = []
+        for ident in active:
+            issued, target = self.batch.status(ident)
+            if issued >= target:
+                done.append(ident)
+        return done
 
     def _retire(self, active: dict, finished: list, t0: float) -> None:
         for ident in finished:
