@@ -437,8 +437,11 @@ def served_measurement(rates, count: int, device: int = 0, arena_bytes: int = 15
     """Poisson arrival traces replayed twice each: continuous batching over
     one arena (admission by bytes, join and leave at 50-step chunk
     boundaries, 8 probes of Ez/Hy per step) and the plain solver, first come
-    first served.  Scene axes log-uniform in [48, 320] cells, steps uniform in
-    [200, 5000].  Latency = completion (results on the host) - arrival."""
+    first served, recording the same probe series.  Scene axes log-uniform in
+    [48, 320] cells, steps uniform in [200, 5000].  Latency = completion
+    (results on the host) - arrival.  Every request's series is compared bit
+    for bit between the two replays."""
+    import numpy as np
     from diaphane_gb300.serve import Server, poisson_trace, serve_plain, summary
     server = Server(arena_bytes, max_scenes=256, chunk_steps=50, device=device)
     warm = dict(lo=48, hi=64, steps=(50, 60))
@@ -450,8 +453,12 @@ def served_measurement(rates, count: int, device: int = 0, arena_bytes: int = 15
         served = summary(trace)
         served["chunks"] = server.chunks
         served["peak_active"] = server.peak_active
-        plain = summary(serve_plain(poisson_trace(count, rate), device))
+        plain_trace = serve_plain(poisson_trace(count, rate), device)
+        plain = summary(plain_trace)
+        same = sum(bool(np.array_equal(a.series.view(np.uint32), b.series.view(np.uint32)))
+                   for a, b in zip(sorted(trace, key=lambda r: r.ident), sorted(plain_trace, key=lambda r: r.ident)))
         out.append({"arrivals_per_s": rate, "served": served, "plain": plain,
+                    "series_identical": same, "series_compared": len(trace),
                     "p99_ratio_plain_over_served": plain["p99_s"] / served["p99_s"],
                     "throughput_ratio": served["solves_per_s"] / plain["solves_per_s"]})
         server.chunks = 0

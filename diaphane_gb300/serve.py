@@ -152,9 +152,9 @@ class Server:
 
 def serve_plain(trace: list[Request], device: int = 0, clock: Callable[[], float] = time.perf_counter
                 ) -> list[Request]:
-    """First come, first served with one ``Simulation`` per request.  The plain
-    solver has no probe gather, so each request ends with a read of its final
-    electric field instead (the same bytes order as a probe series or more)."""
+    """First come, first served with one ``Simulation`` per request, each
+    recording the same probe series as the served form (a probe ring of the
+    request's step count) and reading it back when its last step has run."""
     t0 = clock()
     for r in sorted(trace, key=lambda q: q.arrival):
         now = clock() - t0
@@ -162,8 +162,9 @@ def serve_plain(trace: list[Request], device: int = 0, clock: Callable[[], float
             time.sleep(r.arrival - now)
         r.admitted = clock() - t0
         sim = Simulation(r.resolve(), device=device)
+        sim.set_probes(r.probes, capacity=r.steps)
         sim.advance_by(r.steps)
-        r.series = sim.read_electric()
+        r.series = sim.read_probes(1, r.steps)
         sim.close()
         r.done = clock() - t0
         r.resolved = None

@@ -56,3 +56,15 @@ def test_plain_replay_and_summary():
     trace = serve_plain(poisson_trace(3, rate=1000.0, seed=0x9A1, lo=32, hi=40, steps=(20, 30)))
     s = summary(trace)
     assert s["requests"] == 3 and s["solves_per_s"] > 0 and s["p99_s"] >= s["p50_s"] > 0
+
+
+def test_served_and_plain_replays_return_the_same_series():
+    """The plain replay records the same probes through the solo solver's
+    probe ring: every request's series is the same bits in both."""
+    served = Server(1 << 30, max_scenes=8, chunk_steps=8)
+    a = served.serve(poisson_trace(4, rate=1000.0, seed=0x5A3E, lo=32, hi=44, steps=(20, 36), probe_count=3))
+    served.close()
+    b = serve_plain(poisson_trace(4, rate=1000.0, seed=0x5A3E, lo=32, hi=44, steps=(20, 36), probe_count=3))
+    for x, y in zip(sorted(a, key=lambda r: r.ident), sorted(b, key=lambda r: r.ident)):
+        assert x.series.shape == y.series.shape == (x.steps, 3, 2)
+        assert np.array_equal(x.series.view(np.uint32), y.series.view(np.uint32)), x.ident
