@@ -391,6 +391,13 @@ def batched_measurement(scene_count: int, steps: int, device: int = 0, rank: int
     offsets = np.cumsum([0] + [3 * r.cells for r in resolved])
     plain_out = torch.empty(int(offsets[-1]), dtype=torch.float32, pin_memory=True).numpy()
     batch_out = torch.empty(int(offsets[-1]), dtype=torch.float32, pin_memory=True).numpy()
+    # Set-up, like the allocation: one device-to-host copy into each buffer
+    # faults its freshly pinned pages in for DMA before either clock starts.
+    scratch = torch.zeros(int(offsets[-1]), dtype=torch.float32, device=f"cuda:{device}")
+    for host in (plain_out, batch_out):
+        torch.from_numpy(host).copy_(scratch)
+    del scratch
+    torch.cuda.synchronize(device)
     # Plain: one Simulation per scene, one after another.
     t0 = time.perf_counter()
     for k, r in enumerate(resolved):
