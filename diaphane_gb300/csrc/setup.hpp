@@ -213,7 +213,6 @@ template <typename T> class IncidentLines {
 
 // Waveform::evaluate in T (float and double are instantiated).
 template <typename T> T waveform_in(const dp_waveform &w, T time);
-inline float waveform_value(const dp_waveform &w, float time) { return waveform_in<float>(w, time); }
 float injection_weight(const StepInjection &inj, const float position[3]);
 
 // Shape::contains, src/scene.rs:60-81: membership of a cell centre.
