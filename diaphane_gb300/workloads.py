@@ -8,8 +8,6 @@ from __future__ import annotations
 
 import math
 
-import numpy as np
-
 from .scene import Axis, Boundary, Extent, Grid, Material, Refinement, Scene, Shape, Source, Waveform, f32
 
 MASK = (1 << 64) - 1

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle
-from diaphane_gb300 import DP_KERNEL_FUSED, DP_KERNEL_NAIVE, Axis, Extent, Scene, Simulation
+from diaphane_gb300 import DP_KERNEL_FUSED, DP_KERNEL_NAIVE, Extent, Scene, Simulation
 from tests import scenes
 from tests.helpers import assert_field_parity
 

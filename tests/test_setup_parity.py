@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle
-from diaphane_gb300 import _abi, Axis, Extent, ResolvedScene, Scene, Source, Waveform
+from diaphane_gb300 import _abi, Axis, Extent, ResolvedScene, Scene
 from tests import scenes
 
 TABLES = [_abi.DP_TABLE_MAGNETIC_GAINS, _abi.DP_TABLE_ELECTRIC_GAINS, _abi.DP_TABLE_CELL_CENTERS,
