@@ -462,7 +462,6 @@ dp_status dp_renderer_create(dp_sim *sim, uint32_t width, uint32_t height, dp_re
         r->height = height;
         sim->bind();
         const Scene &s = sim->scene;
-        const uint32_t *n = s.grid.n;
         // The world-to-cell table at the reference GPU solver's sample count.
         r->samples = s.lookup_samples();
         const std::vector<float> lookup = s.cell_lookup(r->samples);

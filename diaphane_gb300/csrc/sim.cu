@@ -78,7 +78,7 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
     auto &owned = sim->owned;
     cudaStream_t st = sim->stream;
 
-    uint32_t requested = opts ? opts->kernel : DP_KERNEL_AUTO;
+    uint32_t requested = opts ? opts->kernel : uint32_t(DP_KERNEL_AUTO);
     if (requested > DP_KERNEL_NAIVE) throw Error(DP_ERR_INVALID, "unknown kernel selector");
     // The fused step stages the coefficient table in shared memory and reads
     // a u8 index through its tensor map: at most 256 materials.
