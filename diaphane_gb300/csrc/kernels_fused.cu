@@ -514,9 +514,12 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         if (__syncthreads_or(!ok)) {
             // Give up on this chunk: report, then let the loads already in
             // flight land before the CTA's shared memory goes away.
+            // Issued so far: the first kSlots planes, then at each later plane
+            // the one kSlots - 1 ahead of the one before (its refill comes below).
             if (threadIdx.x == 0) {
                 atomicExch(u.error, 1);
-                for (int q = p; q <= min(p + kSlots - 1, last_plane); ++q) {
+                const int issued = min(p == zs ? zs + kSlots - 1 : p + kSlots - 2, last_plane);
+                for (int q = p; q <= issued; ++q) {
                     const int kq = (q - zs) % kSlots;
                     mbar_wait_bounded(bar0 + 8 * kq, uint32_t((q - zs) / kSlots) & 1u, kWaitCycles);
                 }
