@@ -1,0 +1,43 @@
+"""`bench.py --impl reference` on the CPU: the reference arm's one JSON line
+keeps the benchmark contract (metric, unit, the warm-up asked for, a
+cpu_baseline naming the port and its cores, an e2e with no host-device
+bytes), on a small grid and a short budget; under torchrun only rank 0
+prints."""
+import json
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent.parent
+
+
+def run(env_extra=None):
+    env = dict(os.environ)
+    env.update(env_extra or {})
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--side", "32", "--steps", "4",
+           "--warmup", "3", "--ref-budget", "2"]
+    return subprocess.run(cmd, capture_output=True, text=True, timeout=600, env=env, cwd=ROOT)
+
+
+def test_reference_arm_prints_one_line_with_the_contract_keys():
+    proc = run()
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    lines = [l for l in proc.stdout.splitlines() if l.strip()]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference"
+    assert line["metric"] == "Gcell-updates/s" and line["unit"] == "Gcell/s"
+    assert line["higher_is_better"] is True and line["value"] > 0
+    assert line["warmup"] == 3 and 1 <= line["steps"] <= 4
+    assert line["config"]["workload"] == "heterogeneous scatterers 32^3"
+    cpu = line["cpu_baseline"]
+    assert cpu["kind"] == "port" and cpu["cores"] >= 1 and cpu["value"] == line["value"]
+    e2e = line["e2e"]
+    assert e2e["value"] == line["value"] and e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+
+
+def test_reference_arm_is_rank_zero_only():
+    proc = run({"WORLD_SIZE": "2", "RANK": "1", "LOCAL_RANK": "1"})
+    assert proc.returncode == 0, proc.stderr[-2000:]
+    assert proc.stdout.strip() == ""
