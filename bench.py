@@ -335,10 +335,10 @@ def run_ours(args):
     cpu = None
     if world == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=12.0, max_steps=200, warmup=0)
+        rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=12.0, max_steps=200, warmup=1)
         rate1, steps1, elapsed1 = cpu_port_rate(scene, 1, budget_s=8.0, max_steps=50, warmup=0)
         cpu = {"value": rate, "unit": "Gcell/s", "cores": threads, "kind": "port",
-               "sample": f"{steps} oracle steps of the same {args.side}^3 scene, {elapsed:.1f} s",
+               "sample": f"{steps} oracle steps of the same {args.side}^3 scene after 1 untimed, {elapsed:.1f} s",
                "single_thread": {"value": rate1, "unit": "Gcell/s", "cores": 1,
                                  "sample": f"{steps1} oracle steps, {elapsed1:.1f} s"},
                "nproc": os.cpu_count(), "cpu_model": cpu_model()}
