@@ -66,3 +66,19 @@ def test_batch_bytes_saturate_instead_of_wrapping():
     assert Batch.bytes_for(resolved, 1 << 62, probe_count=8) == (1 << 64) - 1
     assert Batch.bytes_for(resolved, (1 << 40) // 16, probe_count=8) < 1 << 45
     assert Batch.bytes_for(resolved, 1 << 62, probe_count=0) < 1 << 30
+
+
+def test_header_compiles_as_plain_c_and_cpp(tmp_path):
+    """The boundary is a C ABI: the header must parse as pedantic C99 (what
+    bindgen or cgo read) as well as C++."""
+    import shutil
+    import subprocess
+    import pytest
+    for compiler, std, suffix in (("gcc", "-std=c99", "c"), ("g++", "-std=c++11", "cpp")):
+        if shutil.which(compiler) is None:
+            pytest.skip(f"{compiler} not installed")
+        src = tmp_path / f"h.{suffix}"
+        src.write_text('#include "diaphane_gb300.h"\nint main(void) { return 0; }\n')
+        proc = subprocess.run([compiler, std, "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only",
+                               "-I", str(HEADER.parent), str(src)], capture_output=True, text=True)
+        assert proc.returncode == 0, proc.stderr
