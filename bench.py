@@ -55,6 +55,11 @@ def parse():
     p.add_argument("--variant", default="", help="fused kernel cx,tile_y,slots (default: tuned)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the mixed-size batch measurement")
+    p.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
+    p.add_argument("--no-accuracy", action="store_true", help="skip the FP64 error measurement")
+    p.add_argument("--regime", type=int, default=1000,
+                   help="untimed steps before the warm-up, so the timed window sees the late-regime field "
+                        "(the wave has filled the box and the absorbers hold decaying field)")
     p.add_argument("--workload", choices=["heterogeneous", "batched", "served", "accuracy", "extras", "kernels"],
                    default="heterogeneous")
     p.add_argument("--scenes", type=int, default=256, help="batched: scenes per batch")
@@ -211,11 +216,29 @@ def cpu_model() -> str:
     return platform.processor() or platform.machine()
 
 
+def loaded_libraries() -> list[str]:
+    """The in-tree shared libraries this process has mapped (from
+    /proc/self/maps), relative to the repository root."""
+    found = set()
+    try:
+        for line in Path("/proc/self/maps").read_text().splitlines():
+            path = line.split()[-1] if line.split() else ""
+            if path.endswith(".so") and path.startswith(str(ROOT)):
+                found.add(str(Path(path).relative_to(ROOT)))
+    except OSError:
+        pass
+    return sorted(found)
+
+
 def run_reference(args):
     world, rank, _ = distributed()
     if rank != 0:
         return
-    from diaphane_gb300 import workloads
+    # The scene is built with the oracle's grid resolver, so this process
+    # never loads the CUDA library: the arm is the CPU restatement alone.
+    import oracle
+    from diaphane_gb300 import scene as scene_model, workloads
+    scene_model.use_grid_resolver(oracle.OracleGridResolver)
     threads = os.cpu_count() or 1
     scene = workloads.heterogeneous(args.side)
     rate, steps, elapsed = cpu_port_rate(scene, threads, budget_s=args.ref_budget, max_steps=args.steps,
@@ -230,7 +253,8 @@ def run_reference(args):
                              "nproc": os.cpu_count(), "cpu_model": cpu_model()},
             "e2e": {"value": rate, "unit": "Gcell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference is Rust (cargo absent on both machines); this is the oracle's C++ restatement "
-                    "of src/cpu.rs with OpenMP over z planes"}
+                    "of src/cpu.rs with OpenMP over z planes",
+            "libraries_loaded": loaded_libraries()}
     print(json.dumps(line), flush=True)
 
 
@@ -264,9 +288,11 @@ def run_ours(args):
             import torch.distributed as dist
             dist.barrier()
 
+    sim.advance_by(args.regime)
     sim.advance_by(args.warmup)
-    sim.wait()
+    sim.wait(600_000)
     barrier()
+    first_timed = sim.step_count()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = sim.launch_count()
     with ClockSampler(device) as clocks:
@@ -287,19 +313,21 @@ def run_ours(args):
         pinned_h = torch.empty(3 * cells, dtype=torch.float32, pin_memory=True)
         pinned_i = torch.empty(cells, dtype=torch.float32, pin_memory=True)
         from diaphane_gb300 import Snapshot
-        # Set-up, like the allocation: one copy each way through the same
-        # calls faults the freshly pinned pages in for DMA (measured on GB300:
-        # the first copy into new pinned memory took 0.14 s for 3.8 GB after
-        # a minute of CPU load, every later one 0.02 s).  The buffers are
-        # zeroed again, so the timed run starts from the same state.
+        # Set-up, like the allocation: the late-regime state the device-timed
+        # window ended in is read into the pinned buffers (one copy each way
+        # through the same calls also faults the freshly pinned pages in for
+        # DMA: measured on GB300, the first copy into new pinned memory took
+        # 0.14 s for 3.8 GB after a minute of CPU load, every later one
+        # 0.02 s).  The timed run restores that state from the host and
+        # steps the same regime again.
+        sim.wait(600_000)
+        snap_step = sim.step_count()
         read_into(sim, pinned_i, pinned_e, pinned_h)
-        pinned_e.zero_()
-        pinned_h.zero_()
-        sim.restore(Snapshot(0, pinned_e.numpy(), pinned_h.numpy()))
+        sim.restore(Snapshot(snap_step, pinned_e.numpy(), pinned_h.numpy()))
         sim.wait(600_000)
         barrier()
         t0 = time.perf_counter()
-        sim.restore(Snapshot(0, pinned_e.numpy(), pinned_h.numpy()))
+        sim.restore(Snapshot(snap_step, pinned_e.numpy(), pinned_h.numpy()))
         sim.set_accumulate_intensity(False)
         sim.set_accumulate_intensity(True)
         sim.advance_by(args.steps)
@@ -310,19 +338,31 @@ def run_ours(args):
         d2h = 28 * cells / args.steps
         e2e = {"value": world * cells * args.steps / e2e_s / 1e9, "unit": "Gcell/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-               "what": "restore E,H from pinned host memory; advance K steps with intensity; "
-                       "read intensity, E and H back; wall clock"}
+               "what": "restore E,H (the late-regime state at step %d) from pinned host memory; advance K "
+                       "steps with intensity; read intensity, E and H back; wall clock" % snap_step}
 
     # Every rank takes part in the batch measurement (its scenes, then the
     # slowest rank's time); the rest is rank 0's.
     kernel_name = ["", "fused", "naive"][sim.kernel]
+    accuracy = None
+    if rank == 0 and world == 1 and not args.no_accuracy:
+        try:
+            accuracy = default_accuracy(sim, resolved, device)
+        except Exception as exc:  # reported, not fatal to the headline line
+            accuracy = {"error": f"{type(exc).__name__}: {exc}"}
+    sim.close()
     batched = None
     if not args.no_batched:
-        sim.close()
         try:
             batched = batched_measurement(args.scenes, args.batch_steps, device, rank, world)
         except Exception as exc:  # reported, not fatal to the headline line
             batched = {"error": f"{type(exc).__name__}: {exc}"}
+    served = None
+    if rank == 0 and world == 1 and not args.no_served:
+        try:
+            served = default_served(device, value)
+        except Exception as exc:  # reported, not fatal to the headline line
+            served = {"error": f"{type(exc).__name__}: {exc}"}
     if rank != 0:
         return
     peak, peak_kind = measured_peaks()
@@ -347,8 +387,11 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded SplitMix64 scene)",
             "config": config(args.side, world), "kernel": kernel_name,
             "variant": args.variant or "default",
+            "regime": {"timed_from_step": first_timed,
+                       "what": f"{args.regime} untimed steps and {args.warmup} warm-up steps before the timed "
+                               "window: the wave has crossed the box and the absorbers hold decaying field"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-            "clocks": clocks.summary(), "batched": batched}
+            "clocks": clocks.summary(), "batched": batched, "served": served, "accuracy": accuracy}
     print(json.dumps(line), flush=True)
 
 
@@ -438,6 +481,78 @@ def batched_measurement(scene_count: int, steps: int, device: int = 0, rank: int
             "bit_identical_to_plain": all(identical), "scenes_compared": len(identical),
             "scenes_identical": sum(identical), "replicas": world,
             "scaling": "strong (the 256 scenes are split across replicas)"}
+
+
+def default_accuracy(sim, resolved, device: int) -> dict:
+    """FP64 error of the configurations the line stands for, on the GPU:
+    the metric's 512³ scene at the step this run ended on (the f32 fields of
+    the benchmarked simulation against the FP64 instance stepped as far),
+    free flight 80³ at 1000 steps normalized by the launched peak, and a
+    sample of the mixed-size batch's scenes at 1000 steps."""
+    from diaphane_gb300 import Simulation64, workloads
+    steps = sim.step_count()
+    f64 = Simulation64(resolved, device=device)
+    f64.advance_by(steps)
+    f64.wait(1_800_000)
+    e32, e64 = sim.energy().total(), f64.energy().total()
+    metric = {"case": WORKLOAD, "steps": steps,
+              "E": field_error(sim.read_electric(), f64.read_electric()),
+              "H": field_error(sim.read_magnetic(), f64.read_magnetic()),
+              "energy_rel_diff": abs(e32 - e64) / e64 if e64 else None,
+              "normalization": "max |f32 - f64| over all three components / max |f64| at that step"}
+    f64.close()
+    return {"heterogeneous_512": metric, "free_flight_80": free_flight_accuracy(device),
+            "batched_sample": [accuracy_case(f"mixed scene {k}", workloads.mixed_scene(BATCH_SEED + k), 1000, device)
+                               for k in range(3)]}
+
+
+def free_flight_accuracy(device: int = 0, steps: int = 1000, every: int = 50) -> dict:
+    """Free flight 80³: the f32 step and the FP64 instance side by side.  The
+    packet leaves through the absorber, so the error is stated against the
+    launched peak (the largest |E| of the FP64 run at any sampled step), at
+    the end and at its worst over the run."""
+    import numpy as np
+    from diaphane_gb300 import ResolvedScene, Simulation, Simulation64, workloads
+    resolved = ResolvedScene(workloads.free_flight(80))
+    f32, f64 = Simulation(resolved, device=device), Simulation64(resolved, device=device)
+    launched, worst, last = 0.0, 0.0, 0.0
+    for _ in range(steps // every):
+        f32.advance_by(every)
+        f64.advance_by(every)
+        a, b = f32.read_electric().astype(np.float64), f64.read_electric()
+        launched = max(launched, float(np.abs(b).max()))
+        last = float(np.abs(a - b).max())
+        worst = max(worst, last)
+    f32.close()
+    f64.close()
+    return {"case": "free flight 80^3", "steps": steps, "launched_peak": launched,
+            "E_at_end_of_launched_peak": last / launched, "E_worst_of_launched_peak": worst / launched,
+            "normalization": f"max |f32 - f64| of E / the largest |E| of the FP64 run, sampled every {every} steps"}
+
+
+def default_served(device: int, plain_rate_gcells: float, rate: float = 16.0, count: int = 48) -> dict:
+    """One Poisson trace (48 requests at 16/s) served by continuous batching
+    and by the plain solver, with the ceilings that bound it: the trace's
+    cell-updates at the single-scene 512³ rate, and the arrivals themselves."""
+    results = served_measurement([rate], count, device)[0]
+    from diaphane_gb300.serve import poisson_trace
+    trace = poisson_trace(count, rate)
+    cell_updates = 0
+    for r in trace:
+        r.resolve()
+        cell_updates += r.cells * r.steps
+        r.resolved = None
+    stepping_s = cell_updates / (plain_rate_gcells * 1e9)
+    last_arrival = max(r.arrival for r in trace)
+    results["ceiling"] = {
+        "cell_updates": cell_updates,
+        "stepping_s_at_512_rate": stepping_s,
+        "solves_per_s_at_512_rate": count / stepping_s,
+        "last_arrival_s": last_arrival,
+        "what": "the trace's cell-updates at this run's plain 512^3 rate bound solves/s from above (the plain "
+                "solver already runs its large requests near that rate); arrivals end at last_arrival_s"}
+    results["ceiling"]["speedup_bound_over_plain"] = (count / stepping_s) / results["plain"]["solves_per_s"]
+    return results
 
 
 def run_batched(args):
@@ -695,11 +810,11 @@ def kernels_measurement(side: int = 256, device: int = 0) -> dict:
 
 def run_accuracy(args):
     from diaphane_gb300 import workloads
-    cases = [accuracy_case("free flight 80^3", workloads.free_flight(80), 1000),
-             accuracy_case("heterogeneous 512^3", workloads.heterogeneous(512), 2000),
+    cases = [accuracy_case("heterogeneous 512^3", workloads.heterogeneous(512), 2000),
              accuracy_case("graded stack 640x256x256", workloads.graded_stack(), 5000)]
+    cases += [accuracy_case(f"mixed scene {k}", workloads.mixed_scene(BATCH_SEED + k), 1000) for k in range(8)]
     line = {"metric": "f32 error against the FP64 instance", "workload": "accuracy", "cases": cases,
-            "drift": drift_case()}
+            "free_flight": free_flight_accuracy(), "drift": drift_case()}
     print(json.dumps(line), flush=True)
 
 

@@ -164,7 +164,8 @@ SIGNATURES = [
     ("dp_batch_memory", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("dp_scene_batch_bytes", C.c_uint64, [_P, C.c_uint32, C.c_uint64]),
     ("dp_batch_launch_count", C.c_uint64, [_P]),
-    ("dp_energy_noalloc", C.c_int, [_P, _P, _P, _P, _P, _P, C.POINTER(C.c_uint32), _P, _P]),
+    ("dp_energy_noalloc", C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P, _P,
+                                     C.POINTER(C.c_uint32), _P, _P]),
     ("dp_sim_kernel", C.c_uint32, [_P]),
     ("dp_sim_row_pitch", C.c_uint32, [_P]),
     ("dp_sim_launch_count", C.c_uint64, [_P]),

@@ -185,5 +185,8 @@ size_t fused_variant_smem(uint32_t cx, uint32_t tile_y, uint32_t slots);
 void configure_batch_kernels();
 // Whether tensor maps can be encoded at all (driver entry point present).
 bool tensor_maps_available();
+// Test hook: the fused kernels' plane-wait budget on the current device, in
+// clock cycles (negative: the default bound; 0: give up at the first plane).
+void set_ring_wait_budget(long long cycles);
 
 } // namespace diaphane

@@ -53,6 +53,12 @@ namespace {
 constexpr int kMaxMaterials = 256;
 constexpr long long kWaitCycles = 1ll << 32; // ~2 s at 2 GHz, then give up
 
+// The budget of the plane waits, in clock cycles: kWaitCycles, unless a test
+// lowers it to show the give-up path on the device (0 gives up at the first
+// plane).  The drain after a give-up always keeps the full bound, so every
+// load a CTA issued lands before it exits.
+__device__ long long g_ring_wait_budget = kWaitCycles;
+
 // CX cells per lane along x, TY rows per tile (one warp each), SLOTS planes
 // in the shared-memory ring.
 template <int CX, int TY, int SLOTS> struct Geometry {
@@ -502,15 +508,16 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
 #pragma unroll
     for (int j = 0; j < CX; ++j) hx_prev.v[j] = hy_prev.v[j] = 0.0f;
 
+    const long long ring_budget = g_ring_wait_budget;
     for (int p = zs; p < z1; ++p) {
         const int k = (p - zs) % kSlots, k1 = (p + 1 - zs) % kSlots;
         const uint32_t phase = uint32_t((p - zs) / kSlots) & 1u, phase1 = uint32_t((p + 1 - zs) / kSlots) & 1u;
         // Every thread waits on the ring itself: a lone poller followed by a
         // barrier measured ~30% slower (the barrier adds the poller's wake-up
         // latency to every plane).
-        bool ok = true;
-        if (p == zs) ok = mbar_wait_bounded(bar0 + 8 * k, phase, kWaitCycles);
-        ok = ok && mbar_wait_bounded(bar0 + 8 * k1, phase1, kWaitCycles);
+        bool ok = ring_budget > 0;
+        if (p == zs) ok = ok && mbar_wait_bounded(bar0 + 8 * k, phase, ring_budget);
+        ok = ok && mbar_wait_bounded(bar0 + 8 * k1, phase1, ring_budget);
         if (__syncthreads_or(!ok)) {
             // Give up on this chunk: report, then let the loads already in
             // flight land before the CTA's shared memory goes away.
@@ -1078,6 +1085,15 @@ void configure_batch_kernels() {
 }
 
 bool tensor_maps_available() { return encoder() != nullptr; }
+
+void set_ring_wait_budget(long long cycles) {
+    const long long budget = cycles < 0 ? kWaitCycles : cycles;
+    const cudaError_t err = cudaMemcpyToSymbol(g_ring_wait_budget, &budget, sizeof(budget));
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        throw std::runtime_error(std::string("setting the ring wait budget: ") + cudaGetErrorString(err));
+    }
+}
 
 void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, const BatchScene *scenes,
                        const BatchUnit *units, uint32_t unit_count, const DeviceInjection *injections,

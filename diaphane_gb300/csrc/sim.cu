@@ -375,6 +375,24 @@ dp_status dp_internal_raise_wait_error(dp_sim *sim) {
     });
 }
 
+// Not in the public header: sets the fused kernels' plane-wait budget on the
+// simulation's device (cycles; negative restores the default, 0 makes every
+// plane wait give up at once), so a test can make a wait run out on the GPU
+// and watch the kernel report it, drain its loads and exit.
+dp_status dp_internal_ring_wait_budget(dp_sim *sim, long long cycles) {
+    return guarded([&] {
+        if (!sim) throw Error(DP_ERR_INVALID, "null handle");
+        sim->bind();
+        check(cudaStreamSynchronize(sim->stream), "ring wait budget");
+        try {
+            set_ring_wait_budget(cycles);
+        } catch (const std::runtime_error &e) {
+            throw Error(DP_ERR_CUDA, e.what());
+        }
+        return DP_OK;
+    });
+}
+
 dp_status dp_sim_energy_density(dp_sim *sim, float *host, size_t count) {
     return guarded([&] {
         if (!sim || !host) throw Error(DP_ERR_INVALID, "null argument");

@@ -9,7 +9,8 @@ Mirrors the Rust types a caller of the reference builds a run from —
 All arithmetic a preset performs is done in float32, in the reference's
 order, so a preset built here describes exactly the scene the Rust one does.
 Grid quantities that need the resolved (possibly graded) spacing come from
-the library's host-only ``dp_grid_resolve``.
+the library's host-only ``dp_grid_resolve`` (``use_grid_resolver`` swaps in
+another implementation of the same query).
 """
 from __future__ import annotations
 
@@ -87,6 +88,33 @@ class Refinement:
         return Refinement(tuple(center), tuple(extent), cell_size)
 
 
+class LibraryGridResolver:
+    """Grid::build and the grid queries through the library's host-only
+    dp_grid_resolve / dp_grid_map (no device is touched)."""
+
+    @staticmethod
+    def resolve(spec: _abi.dp_grid_spec, out: _abi.dp_grid_info) -> None:
+        _abi.check(_abi.lib().dp_grid_resolve(C.byref(spec), C.byref(out)))
+
+    @staticmethod
+    def map(spec: _abi.dp_grid_spec, op: int, src, dst) -> None:
+        _abi.check(_abi.lib().dp_grid_map(C.byref(spec), op, src, dst))
+
+
+_grid_resolver = LibraryGridResolver
+
+
+def use_grid_resolver(resolver) -> object:
+    """Sets what resolves grid recipes (an object with ``resolve(spec, out)``
+    and ``map(spec, op, src, dst)`` filling the ABI structs) and returns the
+    previous one.  The library's own is the default; a process that must not
+    load the CUDA library at all (a CPU-only baseline) installs another that
+    computes the same values."""
+    global _grid_resolver
+    previous, _grid_resolver = _grid_resolver, resolver
+    return previous
+
+
 @dataclass
 class Grid:
     """The recipe of a Grid (GridSpec, src/grid.rs:381-392); resolved lazily."""
@@ -135,7 +163,7 @@ class Grid:
     def info(self) -> _abi.dp_grid_info:
         spec, keep = self.spec()
         out = _abi.dp_grid_info()
-        _abi.check(_abi.lib().dp_grid_resolve(C.byref(spec), C.byref(out)))
+        _grid_resolver.resolve(spec, out)
         del keep
         return out
 
@@ -143,7 +171,7 @@ class Grid:
         spec, keep = self.spec()
         src = _abi.F3(*values)
         dst = _abi.F3()
-        _abi.check(_abi.lib().dp_grid_map(C.byref(spec), op, src, dst))
+        _grid_resolver.map(spec, op, src, dst)
         del keep
         return (dst[0], dst[1], dst[2])
 

@@ -368,17 +368,28 @@ uint64_t dp_batch_launch_count(const dp_batch *batch);
  * device or fail under memory pressure; some hosts own all device memory
  * through their own allocator).  Computes what dp_sim_energy does, on the
  * calling thread's current device and the given stream (NULL: default
- * stream): electric/magnetic are 3*cells f32, material_index cells u8,
- * eps_mu 2 f32 (relative permittivity, permeability) per material, primary
- * and dual nx+ny+nz f32 each, out 2 f64 (electric, magnetic) — all device
- * pointers.  Its partial sums live in a fixed 64 KiB array inside the
- * library, so it covers at most 2^28 cells (DP_ERR_RANGE beyond).  The first
- * call on a device looks that array's address up; make that first call
- * before any stream capture.  Every call shares the array: calls whose
- * kernels overlap on the GPU race and must be serialized by the caller. */
-dp_status dp_energy_noalloc(const float *electric, const float *magnetic, const uint8_t *material_index,
-                            const float *eps_mu, const float *primary, const float *dual,
-                            const uint32_t extent[3], double *out, void *stream);
+ * stream).  All pointers are device pointers:
+ *   electric, magnetic  3 components of f32 with rows of field_pitch cells
+ *                       (0 = nx): cell (x, y, z) of component a at
+ *                       a*field_pitch*ny*nz + (z*ny + y)*field_pitch + x,
+ *                       the layout dp_sim_device_ptr / dp_sim_row_pitch give;
+ *   material_index      index_bytes (1: u8, 2: u16 for scenes of more than
+ *                       256 materials) per cell, rows of index_pitch cells
+ *                       (0 = nx);
+ *   eps_mu              2 f32 (relative permittivity, permeability) for each
+ *                       of material_count materials; an index at or past
+ *                       material_count makes both sums NaN;
+ *   primary, dual       nx+ny+nz f32 each;
+ *   out                 2 f64 (electric, magnetic).
+ * Its partial sums live in a fixed 64 KiB array inside the library, so it
+ * covers at most 2^28 cells (DP_ERR_RANGE beyond).  The first call on a
+ * device loads the library's device code there; make it before any stream
+ * capture.  Every call shares the array: calls whose kernels overlap on the
+ * GPU race and must be serialized by the caller. */
+dp_status dp_energy_noalloc(const float *electric, const float *magnetic, uint32_t field_pitch,
+                            const void *material_index, uint32_t index_bytes, uint32_t index_pitch,
+                            const float *eps_mu, uint32_t material_count, const float *primary,
+                            const float *dual, const uint32_t extent[3], double *out, void *stream);
 /* Row stride of the device field buffers, in cells. */
 uint32_t dp_sim_row_pitch(const dp_sim *sim);
 /* Kernel the handle actually runs (DP_KERNEL_FUSED or DP_KERNEL_NAIVE). */

@@ -58,6 +58,7 @@ def lib() -> C.CDLL:
             "or_grid_resolve": (C.c_int, [C.POINTER(_abi.dp_grid_spec), C.POINTER(C.c_uint32), C.POINTER(C.c_float),
                                           C.POINTER(C.c_float), C.POINTER(C.c_float), C.POINTER(C.c_float),
                                           C.POINTER(C.c_float)]),
+            "or_grid_info": (C.c_int, [C.POINTER(_abi.dp_grid_spec), C.POINTER(_abi.dp_grid_info)]),
             "or_grid_map": (C.c_int, [C.POINTER(_abi.dp_grid_spec), C.c_int, C.POINTER(C.c_float),
                                       C.POINTER(C.c_float)]),
             "or_numerical_phase_velocity": (C.c_float, [C.c_float, C.c_float, C.POINTER(C.c_float)]),
@@ -265,6 +266,21 @@ def grid_map(grid, op: int, values) -> tuple:
     _check(lib().or_grid_map(C.byref(spec), op, (C.c_float * 3)(*values), out))
     del keep
     return tuple(out)
+
+
+class OracleGridResolver:
+    """Grid recipes resolved by the oracle's own restatement of Grid::build
+    (src/grid.rs:466-594, 695-745), for scene.use_grid_resolver: a process
+    that times the CPU baseline builds its scenes without loading the CUDA
+    library."""
+
+    @staticmethod
+    def resolve(spec, out) -> None:
+        _check(lib().or_grid_info(C.byref(spec), C.byref(out)))
+
+    @staticmethod
+    def map(spec, op: int, src, dst) -> None:
+        _check(lib().or_grid_map(C.byref(spec), op, src, dst))
 
 
 def max_threads() -> int:

@@ -1415,6 +1415,28 @@ int or_grid_resolve(const dp_grid_spec *spec, uint32_t extent_out[3], float *tim
     });
 }
 
+// The resolved grid in the C ABI's own dp_grid_info layout, so that a caller
+// building scenes on the CPU alone (the timed CPU baseline) needs no other
+// library: Grid::{extent, size, time_step, finest, coarsest,
+// reference_cell_size} (src/grid.rs:521-594).
+int or_grid_info(const dp_grid_spec *spec, dp_grid_info *out) {
+    OR_TRY({
+        Grid g = Grid::build(*spec);
+        float worst = 1.0f;
+        for (int a = 0; a < 3; ++a) {
+            out->extent[a] = g.extent[a];
+            out->size[a] = g.size(a);
+            worst = std::fmax(worst, g.spacing[a].worst_ratio());
+        }
+        out->time_step = g.time_step();
+        out->finest = g.finest();
+        out->coarsest = g.coarsest();
+        out->worst_ratio = worst;
+        out->reference_cell_size = g.reference_cell_size();
+        return 0;
+    });
+}
+
 // to_cell / to_position / cell_containing / cell_center through a grid.
 int or_grid_map(const dp_grid_spec *spec, int op, const float in[3], float out[3]) {
     OR_TRY({

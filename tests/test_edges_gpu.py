@@ -143,6 +143,39 @@ def test_a_wait_that_gave_up_is_reported_once_and_the_handle_stays_usable(thread
     assert np.array_equal(bits(sim.read_electric()), bits(ref.read_electric()))
 
 
+def test_a_ring_wait_that_runs_out_on_the_gpu_is_reported_and_the_run_recovers(threads):
+    """The device half of the bounded wait (the reference's host timeout is
+    src/gpu.rs:616-622): with the plane-wait budget set to zero every CTA of a
+    fused step gives up at its first plane, sets the error flag, lets the
+    loads it issued land (the drain keeps its full bound) and exits.  The
+    host reports DP_ERR_TIMEOUT once; after the budget is restored and a
+    snapshot restored, the run continues bit-identical to the oracle."""
+    import ctypes as C
+    from diaphane_gb300 import _abi
+    from diaphane_gb300._abi import DP_ERR_TIMEOUT
+    budget = _abi.lib().dp_internal_ring_wait_budget
+    budget.restype, budget.argtypes = C.c_int, [C.c_void_p, C.c_longlong]
+    scene = small_scene((40, 20, 16))
+    sim = Simulation(scene, kernel=DP_KERNEL_FUSED)
+    sim.advance_by(5)
+    snapshot = sim.snapshot()
+    assert budget(sim.handle, 0) == 0
+    try:
+        sim.advance_by(2)
+        with pytest.raises(DiaphaneError) as err:
+            sim.wait()
+        assert err.value.status == DP_ERR_TIMEOUT
+    finally:
+        assert budget(sim.handle, -1) == 0
+    sim.wait()  # reported once
+    sim.restore(snapshot)
+    sim.advance_by(10)
+    ref = oracle.OracleSimulation(scene, threads=threads)
+    ref.advance_by(15)
+    assert np.array_equal(bits(sim.read_electric()), bits(ref.read_electric()))
+    assert np.array_equal(bits(sim.read_magnetic()), bits(ref.read_magnetic()))
+
+
 def test_autotuning_keeps_the_state_and_the_results(threads):
     """dp_sim_autotune times the fused step's plans from the current state and
     restores it exactly: the run continues bit-identical to the oracle."""
