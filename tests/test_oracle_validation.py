@@ -350,6 +350,29 @@ def test_a_graded_conducting_box_conserves_energy():
     assert drift < 1e-3
 
 
+def test_the_documented_graded_drift_lies_within_the_spread_of_the_windowed_statistic():
+    """Why the oracle's 2.4e-4 and the documented 4.9e-4 differ: the statistic
+    compares two 200-step means of the instantaneous energy, which still
+    beats with the cavity's modes, so where the late window sits moves the
+    figure by several times.  Sliding the late window (steps 20,601-20,800 in
+    tests/graded.rs:315-350) by up to 100 steps either way spans the
+    documented value; a longer window settles an order of magnitude lower."""
+    sim = sim_of(Scene.cavity_on(Grid.graded((0.024,) * 3, 1000.0, [band(4e-3, 0.4e-3)])))
+    sim.advance_by(400)
+    early = mean_energy(sim)
+    sim.advance_by(20_000 - 100)
+    energies = []
+    for _ in range(400):
+        sim.advance()
+        energies.append(sim.energy().total())
+    energies = np.array(energies)
+    drifts = {offset: abs(energies[100 + offset:300 + offset].mean() - early) / early
+              for offset in range(-100, 101, 25)}
+    assert abs(drifts[0] - 2.4e-4) < 0.1e-4, drifts[0]  # the reference's own windows
+    assert min(drifts.values()) < 4.9e-4 < max(drifts.values()), drifts
+    assert max(drifts.values()) < 1e-3  # the asserted bound holds for every placement
+
+
 # ---- total-field box (an extension; pinned by the one-way method above) ---------------
 
 def box_scene(travel: Axis, polarization: Axis, n: int = 48, lo: int = 14, hi: int = 34) -> Scene:
