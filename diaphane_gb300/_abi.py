@@ -12,9 +12,11 @@ LIBRARY = Path(__file__).resolve().parent / "libdiaphane_gb300.so"
 
 DP_OK = 0
 STATUS_NAMES = {0: "DP_OK", 1: "DP_ERR_INVALID", 2: "DP_ERR_LOSSY", 3: "DP_ERR_CUDA", 4: "DP_ERR_TIMEOUT",
-                5: "DP_ERR_OOM", 6: "DP_ERR_UNSUPPORTED", 7: "DP_ERR_RANGE", 8: "DP_ERR_BUSY"}
+                5: "DP_ERR_OOM", 6: "DP_ERR_UNSUPPORTED", 7: "DP_ERR_RANGE", 8: "DP_ERR_BUSY",
+                9: "DP_ERR_NONFINITE"}
 DP_ERR_INVALID, DP_ERR_LOSSY, DP_ERR_CUDA, DP_ERR_TIMEOUT = 1, 2, 3, 4
 DP_ERR_OOM, DP_ERR_UNSUPPORTED, DP_ERR_RANGE, DP_ERR_BUSY = 5, 6, 7, 8
+DP_ERR_NONFINITE = 9
 
 DP_BOUNDARY_PEC, DP_BOUNDARY_ABSORBING = 0, 1
 DP_SHAPE_BLOCK, DP_SHAPE_SPHERE, DP_SHAPE_SLAB = 0, 1, 2
@@ -90,7 +92,7 @@ class dp_injection(C.Structure):
 class dp_batch_options(C.Structure):
     _fields_ = [("device", C.c_int32), ("chunk_steps", C.c_uint32), ("arena_bytes", C.c_uint64),
                 ("max_scenes", C.c_uint32), ("use_graphs", C.c_uint32), ("cells_per_lane", C.c_uint32),
-                ("unit_planes", C.c_uint32)]
+                ("unit_planes", C.c_uint32), ("skip_finite_check", C.c_uint32)]
 
 
 class dp_options(C.Structure):
@@ -159,6 +161,7 @@ SIGNATURES = [
     ("dp_batch_advance_chunk", C.c_int, [_P, C.POINTER(C.c_uint32)]),
     ("dp_batch_wait", C.c_int, [_P, C.c_uint32]),
     ("dp_batch_status", C.c_int, [_P, C.c_uint64, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("dp_batch_fault", C.c_int, [_P, C.c_uint64, C.POINTER(C.c_int), C.POINTER(C.c_uint64)]),
     ("dp_batch_read_field", C.c_int, [_P, C.c_uint64, C.c_uint32, _P, C.c_size_t]),
     ("dp_batch_read_probes", C.c_int, [_P, C.c_uint64, _P, C.c_size_t]),
     ("dp_batch_memory", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
@@ -175,6 +178,10 @@ SIGNATURES = [
     ("dp_sim_energy_density", C.c_int, [_P, _P, C.c_size_t]),
     ("dp_sim_sample", C.c_int, [_P, C.c_uint32, C.c_uint32, C.POINTER(C.c_uint32), C.POINTER(C.c_float)]),
     ("dp_sim_autotune", C.c_int, [_P, C.c_uint32, C.POINTER(dp_tuning)]),
+    ("dp_sim_plan", C.c_int, [_P, C.POINTER(dp_tuning)]),
+    ("dp_tune_cache_export", C.c_int, [C.c_char_p, C.c_size_t, C.POINTER(C.c_size_t)]),
+    ("dp_tune_cache_import", C.c_int, [C.c_char_p]),
+    ("dp_tune_cache_clear", None, []),
     ("dp_sim_set_probes", C.c_int, [_P, _P, C.c_uint32, C.c_uint64]),
     ("dp_sim_read_probes", C.c_int, [_P, C.c_uint64, C.c_uint64, _P, C.c_size_t]),
     ("dp_sim_read_field_async", C.c_int, [_P, C.c_uint32, _P, C.c_size_t]),

@@ -18,9 +18,9 @@ from .simulation import ResolvedScene, _output
 
 class Batch:
     def __init__(self, arena_bytes: int, chunk_steps: int = 50, max_scenes: int = 256, device: int = 0,
-                 use_graphs: bool = True, cells_per_lane: int = 0, unit_planes: int = 0):
+                 use_graphs: bool = True, cells_per_lane: int = 0, unit_planes: int = 0, check_finite: bool = True):
         opts = _abi.dp_batch_options(device, chunk_steps, arena_bytes, max_scenes, int(use_graphs), cells_per_lane,
-                                     unit_planes)
+                                     unit_planes, int(not check_finite))
         handle = C.c_void_p()
         _abi.check(_abi.lib().dp_batch_create(C.byref(opts), C.byref(handle)))
         self.handle = handle
@@ -74,6 +74,14 @@ class Batch:
         step, target = C.c_uint64(), C.c_uint64()
         _abi.check(_abi.lib().dp_batch_status(self.handle, ident, C.byref(step), C.byref(target)))
         return step.value, target.value
+
+    def fault(self, ident: int) -> tuple[int, int]:
+        """(DP_OK, 0), or (DP_ERR_NONFINITE, the step count it stopped at)
+        for a scene whose fields a per-chunk check found NaN or infinite:
+        such a scene has stopped stepping; the others run on."""
+        fault, at = C.c_int(), C.c_uint64()
+        _abi.check(_abi.lib().dp_batch_fault(self.handle, ident, C.byref(fault), C.byref(at)))
+        return fault.value, at.value
 
     def _read(self, ident: int, field: int, count: int, out=None) -> np.ndarray:
         out = _output(out, count)

@@ -128,6 +128,8 @@ struct Entry {
     float *probes = nullptr;      // target × probes × 2 (Ez, Hy)
     std::vector<BatchUnit> units;
     IncidentLines<float> lines;   // the scene's total-field boxes, if any
+    uint64_t joined = 0;          // chunks the batch had started when the scene joined
+    dp_status fault = DP_OK;      // DP_ERR_NONFINITE once a check found a NaN or infinity
 };
 
 // Per-step probe gather: after step t of a chunk, Ez and Hy at every probe
@@ -152,6 +154,31 @@ __global__ void gather_probes(const BatchScene *scenes, const ProbeSlot *slots, 
     const uint64_t at = ((bs.step0 + step) * ps.probes + ps.k) * 2;
     ps.series[at] = ez;
     ps.series[at + 1] = hy;
+}
+
+// is_finite (src/cpu.rs:707-713), per scene, after a chunk: one block per
+// work unit of one variant (tiles `tx` cells wide, 8 rows) reads the unit's
+// cells of all six components in the set the chunk left current and marks
+// the scene's slot when any of them is NaN or infinite.  A mark stays set
+// until the slot is given to another scene.
+__global__ void scan_finite(const BatchScene *scenes, const BatchUnit *units, uint32_t tx, int32_t *marks) {
+    const BatchUnit unit = units[blockIdx.x];
+    const BatchScene &bs = scenes[unit.scene];
+    if (bs.steps == 0) return;
+    const uint32_t set = (bs.parity + bs.steps) & 1u;
+    const uint32_t ny = bs.s.n[1];
+    const uint32_t width = min(tx, bs.s.n[0] - unit.x0), rows = min(8u, ny - unit.y0);
+    const uint32_t per_plane = width * rows, planes = unit.z1 - unit.z0;
+    const uint32_t items = 6u * planes * per_plane;
+    bool bad = false;
+    for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
+        const uint32_t within = i % per_plane, rest = i / per_plane;
+        const uint32_t z = unit.z0 + rest % planes, c = rest / planes;
+        const uint64_t at = (uint64_t(z) * ny + unit.y0 + within / width) * bs.s.pitch + unit.x0 + within % width;
+        const float *f = c < 3 ? bs.e[set] + uint64_t(c) * bs.s.cells : bs.h[set] + uint64_t(c - 3) * bs.s.cells;
+        bad = bad || !isfinite(f[at]);
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) marks[unit.scene] = 1;
 }
 
 void make_units(Entry &e, uint32_t planes);
@@ -189,6 +216,15 @@ struct dp_batch {
     std::vector<cudaEvent_t> joins;
     cudaEvent_t fork = nullptr;
     int32_t *error = nullptr;
+    // Non-finite marks per slot (device), copied after every chunk into the
+    // pinned area of that chunk's staging half, with the event that says the
+    // copy has landed and the number of the chunk it belongs to.
+    bool check_finite = true;
+    int32_t *marks = nullptr;
+    int32_t *h_marks[2] = {nullptr, nullptr};
+    cudaEvent_t marked[2] = {nullptr, nullptr};
+    bool marks_pending[2] = {false, false};
+    uint64_t marks_chunk[2] = {0, 0};
     // Host staging (pinned), double-buffered against in-flight copies.
     BatchScene *h_scenes[2] = {nullptr, nullptr};
     DeviceInjection *h_injections[2] = {nullptr, nullptr};
@@ -221,6 +257,7 @@ struct dp_batch {
         cudaFree(counts);
         cudaFree(probe_slots);
         cudaFree(error);
+        cudaFree(marks);
         for (cudaStream_t l : lanes) cudaStreamDestroy(l);
         for (cudaEvent_t e : joins) cudaEventDestroy(e);
         if (fork) cudaEventDestroy(fork);
@@ -231,7 +268,9 @@ struct dp_batch {
             cudaFreeHost(h_scenes[k]);
             cudaFreeHost(h_injections[k]);
             cudaFreeHost(h_counts[k]);
+            cudaFreeHost(h_marks[k]);
             if (staged[k]) cudaEventDestroy(staged[k]);
+            if (marked[k]) cudaEventDestroy(marked[k]);
         }
         if (stream) cudaStreamDestroy(stream);
     }
@@ -358,13 +397,51 @@ struct dp_batch {
                     ++launches;
                 }
             }
+            if (check_finite && unit_counts[v]) {
+                scan_finite<<<unit_counts[v], 256, 0, lane>>>(scenes, units[v], 32 * variants[v].cx, marks);
+                ++launches;
+            }
             check(cudaEventRecord(joins[v], lane), "join");
             check(cudaStreamWaitEvent(stream, joins[v], 0), "join");
+        }
+        if (check_finite)
+            check(cudaMemcpyAsync(h_marks[half], marks, size_t(capacity) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                  stream),
+                  "finite marks");
+    }
+
+    // Applies the marks of finished chunks: a scene found non-finite stops
+    // stepping (its target becomes the steps issued for it) and reports
+    // DP_ERR_NONFINITE; the others run on untouched, each scene's arithmetic
+    // being its own.  `wait_half` (0 or 1) is waited for, the other half only
+    // taken when its copy has already landed; -1 waits for both, -2 for
+    // neither.
+    void collect_marks(int wait_half) {
+        for (int half = 0; half < 2; ++half) {
+            if (!marks_pending[half]) continue;
+            if (wait_half == -1 || half == wait_half) {
+                check(cudaEventSynchronize(marked[half]), "finite marks");
+            } else {
+                const cudaError_t q = cudaEventQuery(marked[half]);
+                if (q == cudaErrorNotReady) continue;
+                check(q, "finite marks");
+            }
+            marks_pending[half] = false;
+            for (auto &kv : entries) {
+                Entry &e = kv.second;
+                if (e.fault != DP_OK || e.joined > marks_chunk[half] || !h_marks[half][e.slot]) continue;
+                e.fault = DP_ERR_NONFINITE;
+                e.target = e.step;
+            }
         }
     }
 
     // One chunk: stage descriptors and injections, then replay (or launch).
     uint32_t run_chunk() {
+        // The marks of the chunk two back (whose staging half this one
+        // reuses) are waited for, so a scene that turned non-finite stops
+        // within two chunks; the chunk in between keeps the GPU busy.
+        collect_marks(stage);
         // A chunk right after a membership change launches directly: a graph
         // pays off only once it is replayed, and membership that changes
         // every chunk (requests arriving and leaving) would never replay one.
@@ -454,10 +531,17 @@ struct dp_batch {
                 uint64_t per_step = variants.size();
                 for (uint32_t c : probe_count_v) per_step += c ? 1 : 0;
                 launches += uint64_t(chunk) * per_step;
+                if (check_finite)
+                    for (uint32_t c : unit_counts) launches += c ? 1 : 0;
             } else {
                 record_chunk(half);
             }
             check(cudaGetLastError(), "chunk launch");
+            if (check_finite) {
+                check(cudaEventRecord(marked[half], stream), "finite marks");
+                marks_pending[half] = true;
+                marks_chunk[half] = chunks_run;
+            }
         }
         for (auto &kv : entries) {
             Entry &e = kv.second;
@@ -477,6 +561,7 @@ struct dp_batch {
             if (std::chrono::steady_clock::now() >= deadline) throw Error(DP_ERR_TIMEOUT, "the batch did not finish in time");
             std::this_thread::sleep_for(std::chrono::microseconds(50));
         }
+        collect_marks(-1);
         int32_t code = 0;
         check(cudaMemcpy(&code, error, sizeof(code), cudaMemcpyDeviceToHost), "error flag");
         if (code) {
@@ -582,7 +667,13 @@ dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out) {
             check(cudaMallocHost(&b->h_counts[k], b->count_span() * sizeof(uint32_t)), "staging");
             check(cudaEventCreateWithFlags(&b->staged[k], cudaEventDisableTiming), "event");
             check(cudaEventRecord(b->staged[k], b->stream), "event");
+            check(cudaMallocHost(&b->h_marks[k], size_t(b->capacity) * sizeof(int32_t)), "staging");
+            std::memset(b->h_marks[k], 0, size_t(b->capacity) * sizeof(int32_t));
+            check(cudaEventCreateWithFlags(&b->marked[k], cudaEventDisableTiming), "event");
         }
+        b->check_finite = opts->skip_finite_check == 0;
+        check(cudaMalloc(&b->marks, size_t(b->capacity) * sizeof(int32_t)), "finite marks");
+        check(cudaMemset(b->marks, 0, size_t(b->capacity) * sizeof(int32_t)), "finite marks");
         *out = b.release();
         return DP_OK;
     });
@@ -614,6 +705,9 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         e.lines = IncidentLines<float>(s);
         e.slot = slot;
         e.variant = variant_for(s.grid.n[0], b->cells_per_lane);
+        TunedPlan tuned{};
+        if (b->cells_per_lane == 0 && tuned_plan(s.grid.n, b->sm_count, tuned) && tuned.tile_y == 8)
+            e.variant = variant_for(s.grid.n[0], tuned.cx); // the tile width tuned for this shape
         e.pitch = l.pitch;
         e.material_pitch = l.material_pitch;
         e.cells_padded = l.cells;
@@ -644,6 +738,8 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         // Zeroed fields; tables uploaded; the index padded row by row.
         cudaStream_t st = b->stream;
         check(cudaMemsetAsync(b->arena_base + offset, 0, 4 * l.fields + l.intensity, st), "zero fields");
+        check(cudaMemsetAsync(b->marks + slot, 0, sizeof(int32_t), st), "finite mark");
+        e.joined = b->chunks_run;
         rasterize_on_device(s, material, l.material_pitch, st);
         std::vector<float4> table(256, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         for (size_t m = 0; m < s.coefficients.size(); ++m)
@@ -732,6 +828,19 @@ dp_status dp_batch_status(dp_batch *b, uint64_t id, uint64_t *step, uint64_t *ta
         if (it == b->entries.end()) throw Error(DP_ERR_RANGE, "no such scene in the batch");
         *step = it->second.step;
         *target = it->second.target;
+        return DP_OK;
+    });
+}
+
+dp_status dp_batch_fault(dp_batch *b, uint64_t id, dp_status *fault, uint64_t *at_step) {
+    return guarded([&] {
+        if (!b || !fault) throw Error(DP_ERR_INVALID, "null argument");
+        auto it = b->entries.find(id);
+        if (it == b->entries.end()) throw Error(DP_ERR_RANGE, "no such scene in the batch");
+        b->bind();
+        b->collect_marks(-2); // the marks of chunks that have finished; no wait
+        *fault = it->second.fault;
+        if (at_step) *at_step = it->second.fault == DP_OK ? 0 : it->second.step;
         return DP_OK;
     });
 }

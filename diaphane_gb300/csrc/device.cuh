@@ -128,6 +128,17 @@ struct FusedPlan {
     uint32_t grid;        // CTAs launched
     size_t smem;          // dynamic shared memory per CTA
 };
+// Plans dp_sim_autotune found fastest, per grid extent and device SM count,
+// for the life of the process (tune.cu).  A simulation created for that
+// shape with no plan options starts from it; a batch scene of that shape
+// takes its tile width.
+struct TunedPlan {
+    uint32_t cx, tile_y, slots, z_chunk;
+    float ms_per_step;
+};
+bool tuned_plan(const uint32_t n[3], int sms, TunedPlan &out);
+void remember_tuned_plan(const uint32_t n[3], int sms, const TunedPlan &plan);
+
 // Opaque 128-byte CUtensorMap images for one input field set.
 struct FusedMaps {
     alignas(64) unsigned char e[128];

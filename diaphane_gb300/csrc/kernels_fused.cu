@@ -86,7 +86,12 @@ template <int CX, int TY, int SLOTS> struct Geometry {
     static constexpr int SCRATCH_OFF = (BAR_OFF + kSlots * 8 + 15) & ~15;
     static constexpr int SCRATCH_WARP = 2 * kCompactItems * 4;
     static constexpr int INJ_OFF = SCRATCH_OFF + kWarps * SCRATCH_WARP; // 16-aligned
-    static constexpr int SMEM = INJ_OFF + kMaxInjections * int(sizeof(DeviceInjection));
+    // The z-profile samples of a chunk's planes (magnetic gain, electric gain,
+    // absorber at the integer and the half position), one float4 per plane,
+    // for chunks of up to kZPlanes planes.
+    static constexpr int kZPlanes = 64;
+    static constexpr int ZP_OFF = (INJ_OFF + kMaxInjections * int(sizeof(DeviceInjection)) + 15) & ~15;
+    static constexpr int SMEM = ZP_OFF + kZPlanes * 16;
 };
 
 struct FusedArgs {
@@ -432,6 +437,18 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         for (int p = zs; p <= min(zs + kSlots - 1, last_plane); ++p) issue(p);
     }
     for (int m = threadIdx.x; m < kMaxMaterials; m += kThreads) coeff[m] = __ldg(&s.coeff[m]);
+    // The chunk's z-profile samples, staged with the table: one shared load
+    // per plane instead of four dependent global ones.
+    float4 *zprof = reinterpret_cast<float4 *>(smem + G::ZP_OFF);
+    const bool zstaged = z1 - zs <= G::kZPlanes;
+    if (zstaged) {
+        const int off = int(s.n[0] + s.n[1]);
+        const float *ai = s.absorber, *ah = s.absorber + (s.n[0] + s.n[1] + s.n[2]);
+        for (int i = threadIdx.x; i < z1 - zs; i += kThreads) {
+            const int q = off + zs + i;
+            zprof[i] = make_float4(__ldg(&s.mgain[q]), __ldg(&s.egain[q]), __ldg(&ai[q]), __ldg(&ah[q]));
+        }
+    }
     {
         constexpr int kWords = int(sizeof(DeviceInjection) / 4);
         const uint32_t *from = reinterpret_cast<const uint32_t *>(u.inj.item);
@@ -548,8 +565,14 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         auto h_at = [&](float *base, int c, int r, int cc) { return base + (c * G::HR + r) * G::W + cc; };
 
         const bool prologue = p < z0;
-        const float mgz = __ldg(&s.mgain[nx + ny + p]), egz = __ldg(&s.egain[nx + ny + p]);
-        const float aiz = __ldg(&absorb_int[nx + ny + p]), ahz = __ldg(&absorb_half[nx + ny + p]);
+        float mgz, egz, aiz, ahz;
+        if (zstaged) {
+            const float4 zv = zprof[p - zs];
+            mgz = zv.x, egz = zv.y, aiz = zv.z, ahz = zv.w;
+        } else {
+            mgz = __ldg(&s.mgain[nx + ny + p]), egz = __ldg(&s.egain[nx + ny + p]);
+            aiz = __ldg(&absorb_int[nx + ny + p]), ahz = __ldg(&absorb_half[nx + ny + p]);
+        }
         const uint64_t at = (uint64_t(p) * ny + uint64_t(y)) * pitch + xl; // this lane's first cell
 
         // Intensity of this thread's cells, fetched early.

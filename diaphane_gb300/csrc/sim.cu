@@ -139,8 +139,16 @@ dp_sim *make_sim(const Scene &scene, const dp_options *opts) {
         int sms = 0;
         check(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, sim->device), "attribute");
         try {
-            sim->plan = fused_plan(s.grid.n, opts ? opts->cells_per_lane : 0, opts ? opts->tile_y : 0,
-                                   opts ? opts->ring_slots : 0, opts ? opts->z_chunk : 0, sms);
+            // A plan tuned for this shape earlier in the process, unless the
+            // options ask for a particular one.
+            const bool defaults = !opts || (opts->cells_per_lane == 0 && opts->tile_y == 0 &&
+                                            opts->ring_slots == 0 && opts->z_chunk == 0);
+            TunedPlan tuned{};
+            if (defaults && tuned_plan(s.grid.n, sms, tuned))
+                sim->plan = fused_plan(s.grid.n, tuned.cx, tuned.tile_y, tuned.slots, tuned.z_chunk, sms);
+            else
+                sim->plan = fused_plan(s.grid.n, opts ? opts->cells_per_lane : 0, opts ? opts->tile_y : 0,
+                                       opts ? opts->ring_slots : 0, opts ? opts->z_chunk : 0, sms);
         } catch (const std::exception &e) {
             throw Error(DP_ERR_UNSUPPORTED, e.what());
         }

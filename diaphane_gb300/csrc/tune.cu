@@ -10,7 +10,22 @@
 // exactly before every trial and after the last, so tuning changes no result.
 #include "sim.hpp"
 
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <tuple>
+
 namespace {
+
+// The tuned plans of this process: (nx, ny, nz, SM count) -> plan.
+using ShapeKey = std::tuple<uint32_t, uint32_t, uint32_t, int>;
+std::mutex g_tuned_mutex;
+std::map<ShapeKey, diaphane::TunedPlan> g_tuned;
+
+ShapeKey key_of(const uint32_t n[3], int sms) { return ShapeKey{n[0], n[1], n[2], sms}; }
 
 struct Candidate {
     uint32_t cx, ty, slots, z_chunk;
@@ -65,6 +80,23 @@ void use_plan(dp_sim *sim, const FusedPlan &plan) {
 }
 
 } // namespace
+
+namespace diaphane {
+
+bool tuned_plan(const uint32_t n[3], int sms, TunedPlan &out) {
+    std::lock_guard<std::mutex> lock(g_tuned_mutex);
+    auto it = g_tuned.find(key_of(n, sms));
+    if (it == g_tuned.end()) return false;
+    out = it->second;
+    return true;
+}
+
+void remember_tuned_plan(const uint32_t n[3], int sms, const TunedPlan &plan) {
+    std::lock_guard<std::mutex> lock(g_tuned_mutex);
+    g_tuned[key_of(n, sms)] = plan;
+}
+
+} // namespace diaphane
 
 extern "C" dp_status dp_sim_autotune(dp_sim *sim, uint32_t steps, dp_tuning *out) {
     return guarded([&] {
@@ -151,7 +183,73 @@ extern "C" dp_status dp_sim_autotune(dp_sim *sim, uint32_t steps, dp_tuning *out
         result.z_chunk = best.z_chunk;
         result.ms_per_step = best_ms;
         result.candidates = tried;
+        if (tried) remember_tuned_plan(n, sms, TunedPlan{best.cx, best.tile_y, best.slots, best.z_chunk, best_ms});
         if (out) *out = result;
         return DP_OK;
     });
+}
+
+extern "C" dp_status dp_sim_plan(const dp_sim *sim, dp_tuning *out) {
+    return guarded([&] {
+        if (!sim || !out) throw Error(DP_ERR_INVALID, "null argument");
+        dp_tuning t{};
+        if (sim->kernel == DP_KERNEL_FUSED) {
+            t.cells_per_lane = sim->plan.cx;
+            t.tile_y = sim->plan.tile_y;
+            t.ring_slots = sim->plan.slots;
+            t.z_chunk = sim->plan.z_chunk;
+        }
+        *out = t;
+        return DP_OK;
+    });
+}
+
+// One line per shape: "nx ny nz sms cx tile_y slots z_chunk ms_per_step".
+extern "C" dp_status dp_tune_cache_export(char *buf, size_t cap, size_t *len) {
+    return guarded([&] {
+        if (!len || (cap && !buf)) throw Error(DP_ERR_INVALID, "null argument");
+        std::ostringstream text;
+        {
+            std::lock_guard<std::mutex> lock(g_tuned_mutex);
+            for (const auto &kv : g_tuned) {
+                const TunedPlan &p = kv.second;
+                char line[160];
+                std::snprintf(line, sizeof(line), "%u %u %u %d %u %u %u %u %.6g\n", std::get<0>(kv.first),
+                              std::get<1>(kv.first), std::get<2>(kv.first), std::get<3>(kv.first), p.cx, p.tile_y,
+                              p.slots, p.z_chunk, double(p.ms_per_step));
+                text << line;
+            }
+        }
+        const std::string t = text.str();
+        *len = t.size();
+        if (cap < t.size() + 1) throw Error(DP_ERR_RANGE, "the buffer cannot hold the cache");
+        std::memcpy(buf, t.c_str(), t.size() + 1);
+        return DP_OK;
+    });
+}
+
+extern "C" dp_status dp_tune_cache_import(const char *text) {
+    return guarded([&] {
+        if (!text) throw Error(DP_ERR_INVALID, "null argument");
+        std::istringstream in(text);
+        std::string line;
+        while (std::getline(in, line)) {
+            if (line.find_first_not_of(" \t\r") == std::string::npos) continue;
+            uint32_t n[3], cx, ty, slots, depth;
+            int sms;
+            float ms;
+            char extra;
+            if (std::sscanf(line.c_str(), "%u %u %u %d %u %u %u %u %f %c", &n[0], &n[1], &n[2], &sms, &cx, &ty,
+                            &slots, &depth, &ms, &extra) != 9 ||
+                !fused_variant_exists(cx, ty, slots) || n[0] == 0 || n[1] == 0 || n[2] == 0 || depth > n[2])
+                throw Error(DP_ERR_INVALID, "malformed tuning line: " + line);
+            remember_tuned_plan(n, sms, TunedPlan{cx, ty, slots, depth, ms});
+        }
+        return DP_OK;
+    });
+}
+
+extern "C" void dp_tune_cache_clear(void) {
+    std::lock_guard<std::mutex> lock(g_tuned_mutex);
+    g_tuned.clear();
 }

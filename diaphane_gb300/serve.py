@@ -9,6 +9,12 @@ series (Ez and Hy at every probe cell after every step) is read back.  A
 scene joins and leaves only between chunks, so its result is the same alone
 or in any mix.
 
+Failures stay with their request: a scene whose fields turn NaN or infinite
+is stopped by the batch's per-chunk check (is_finite, src/cpu.rs:707-713) and
+retired as "failed" with the step it stopped at, and a request whose client
+gives up (``cancel_after`` seconds after arrival) leaves the queue, or the
+batch at the next chunk boundary, as "cancelled"; the other requests run on.
+
 ``serve_plain`` replays the same trace against the one-scene-at-a-time solver
 (``Simulation``): first come, first served, each request stepped to the end
 before the next one starts.
@@ -23,8 +29,9 @@ from typing import Callable, Optional
 
 import numpy as np
 
-from ._abi import DiaphaneError, DP_ERR_BUSY, DP_ERR_OOM
+from ._abi import DiaphaneError, DP_ERR_BUSY, DP_ERR_OOM, DP_OK
 from .batch import Batch
+from .scene import Scene
 from .simulation import ResolvedScene, Simulation
 from .workloads import SplitMix64, mixed_scene
 
@@ -38,17 +45,22 @@ class Request:
     probe_count: int = 8
     lo: int = 48                # axis range of the scene, cells
     hi: int = 320
+    scene: Optional[Scene] = None          # an explicit scene instead of the seed's
+    cancel_after: Optional[float] = None   # the client gives up this many seconds after arrival
     # Filled in by a replay.
     resolved: Optional[ResolvedScene] = None
     probes: list = field(default_factory=list)
     cells: int = 0
     admitted: Optional[float] = None
     done: Optional[float] = None
-    series: Optional[np.ndarray] = None   # steps × probes × (Ez, Hy)
+    series: Optional[np.ndarray] = None   # steps × probes × (Ez, Hy); None unless "done"
+    outcome: str = ""                     # "done", "failed" (non-finite fields) or "cancelled"
+    fault_step: Optional[int] = None      # steps run when a failed request was stopped
 
     def resolve(self) -> ResolvedScene:
         if self.resolved is None:
-            self.resolved = ResolvedScene(mixed_scene(self.seed, self.lo, self.hi))
+            scene = self.scene if self.scene is not None else mixed_scene(self.seed, self.lo, self.hi)
+            self.resolved = ResolvedScene(scene)
             n = self.resolved.extent
             self.cells = self.resolved.cells
             rng = SplitMix64(self.seed ^ 0x9B0B_E5)
@@ -58,6 +70,9 @@ class Request:
     @property
     def latency(self) -> float:
         return self.done - self.arrival
+
+    def gave_up(self, now: float) -> bool:
+        return self.cancel_after is not None and now >= self.arrival + self.cancel_after
 
 
 def poisson_trace(count: int, rate: float, seed: int = 0x5E_4E_D0, lo: int = 48, hi: int = 320,
@@ -112,10 +127,26 @@ class Server:
     def _retire(self, active: dict, finished: list, t0: float) -> None:
         for ident in finished:
             r = active.pop(ident)
-            r.series = self.batch.read_probes(ident)  # waits for the chunk that finished it
+            fault, at = self.batch.fault(ident)
+            if fault == DP_OK:
+                r.series = self.batch.read_probes(ident)  # waits for the chunk that finished it
+                r.outcome = "done"
+            else:
+                r.outcome, r.fault_step = "failed", at
             self.batch.remove(ident)
             r.done = self.clock() - t0
             r.resolved = None  # the host copy of the scene is no longer needed
+
+    def _cancel(self, queue: deque, active: dict, now: float) -> None:
+        """Requests whose client has given up leave the queue, or the batch
+        (after the chunk that is running), without a result."""
+        for r in [q for q in queue if q.gave_up(now)]:
+            queue.remove(r)
+            r.outcome, r.done, r.resolved = "cancelled", now, None
+        for ident in [i for i, r in active.items() if r.gave_up(now)]:
+            r = active.pop(ident)
+            self.batch.remove(ident)
+            r.outcome, r.done, r.resolved = "cancelled", now, None
 
     def serve(self, trace: list[Request]) -> list[Request]:
         pending = deque(sorted(trace, key=lambda r: r.arrival))
@@ -126,6 +157,7 @@ class Server:
             now = self.clock() - t0
             while pending and pending[0].arrival <= now:
                 queue.append(pending.popleft())
+            self._cancel(queue, active, now)
             self._admit(queue, active, now)
             self.peak_active = max(self.peak_active, len(active))
             if active:
@@ -136,7 +168,8 @@ class Server:
                 for r in list(pending)[:4]:
                     if r.arrival <= self.clock() - t0 + 0.05:
                         r.resolve()
-                # Wait only when a request's last step was just issued.
+                # Wait only when a request's last step was just issued (or a
+                # failed one was stopped).
                 finished = self._finished(active)
                 if finished:
                     self.batch.wait()
@@ -154,17 +187,27 @@ def serve_plain(trace: list[Request], device: int = 0, clock: Callable[[], float
                 ) -> list[Request]:
     """First come, first served with one ``Simulation`` per request, each
     recording the same probe series as the served form (a probe ring of the
-    request's step count) and reading it back when its last step has run."""
+    request's step count) and reading it back when its last step has run.
+    A request whose client gave up before its turn is skipped; one whose
+    fields end non-finite is "failed"."""
     t0 = clock()
     for r in sorted(trace, key=lambda q: q.arrival):
         now = clock() - t0
         if now < r.arrival:
             time.sleep(r.arrival - now)
-        r.admitted = clock() - t0
+            now = clock() - t0
+        if r.gave_up(now):
+            r.outcome, r.done, r.resolved = "cancelled", now, None
+            continue
+        r.admitted = now
         sim = Simulation(r.resolve(), device=device)
         sim.set_probes(r.probes, capacity=r.steps)
         sim.advance_by(r.steps)
-        r.series = sim.read_probes(1, r.steps)
+        if sim.is_finite():
+            r.series = sim.read_probes(1, r.steps)
+            r.outcome = "done"
+        else:
+            r.outcome, r.fault_step = "failed", r.steps
         sim.close()
         r.done = clock() - t0
         r.resolved = None
@@ -172,11 +215,17 @@ def serve_plain(trace: list[Request], device: int = 0, clock: Callable[[], float
 
 
 def summary(trace: list[Request]) -> dict:
-    lat = np.array([r.latency for r in trace])
+    """Solves per second and completion latency over the requests that
+    were solved; failed and cancelled ones are counted beside them."""
+    solved = [r for r in trace if r.outcome in ("done", "")]
+    lat = np.array([r.latency for r in solved]) if solved else np.zeros(1)
     first = min(r.arrival for r in trace)
     last = max(r.done for r in trace)
-    cell_steps = sum(r.steps * r.cells for r in trace)
-    return {"requests": len(trace), "solves_per_s": len(trace) / (last - first),
+    cell_steps = sum(r.steps * r.cells for r in solved)
+    return {"requests": len(trace), "solved": len(solved),
+            "failed": sum(r.outcome == "failed" for r in trace),
+            "cancelled": sum(r.outcome == "cancelled" for r in trace),
+            "solves_per_s": len(solved) / (last - first),
             "p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "mean_s": float(lat.mean()), "makespan_s": last - first,
             "gcells_per_s": cell_steps / (last - first) / 1e9}

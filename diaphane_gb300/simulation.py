@@ -257,6 +257,14 @@ class Simulation:
         return {"cells_per_lane": t.cells_per_lane, "tile_y": t.tile_y, "ring_slots": t.ring_slots,
                 "z_chunk": t.z_chunk, "ms_per_step": t.ms_per_step, "candidates": t.candidates}
 
+    def plan(self) -> dict:
+        """The fused-step plan the handle runs (all 0 on the
+        one-thread-per-cell path)."""
+        t = _abi.dp_tuning()
+        _abi.check(_abi.lib().dp_sim_plan(self.handle, C.byref(t)))
+        return {"cells_per_lane": t.cells_per_lane, "tile_y": t.tile_y, "ring_slots": t.ring_slots,
+                "z_chunk": t.z_chunk}
+
     # -- probes and asynchronous read-back ---------------------------------------
     def set_probes(self, cells, capacity: int) -> None:
         """Ez and Hy at `cells` ((x, y, z) each) after every step, kept for the
@@ -327,3 +335,24 @@ class Simulation64:
         e, m = C.c_double(), C.c_double()
         _abi.check(_abi.lib().dp_sim64_energy(self.handle, C.byref(e), C.byref(m)))
         return Energy(e.value, m.value)
+
+
+def tuning_cache_export() -> str:
+    """The process's tuned plans as text, one line per grid shape:
+    "nx ny nz sms cells_per_lane tile_y ring_slots z_chunk ms_per_step"."""
+    need = C.c_size_t()
+    status = _abi.lib().dp_tune_cache_export(None, 0, C.byref(need))
+    if status not in (_abi.DP_OK, _abi.DP_ERR_RANGE):
+        _abi.check(status)
+    buf = C.create_string_buffer(need.value + 1)
+    _abi.check(_abi.lib().dp_tune_cache_export(buf, len(buf), C.byref(need)))
+    return buf.value.decode()
+
+
+def tuning_cache_import(text: str) -> None:
+    """Adds exported lines to the process's tuned plans."""
+    _abi.check(_abi.lib().dp_tune_cache_import(text.encode()))
+
+
+def tuning_cache_clear() -> None:
+    _abi.lib().dp_tune_cache_clear()

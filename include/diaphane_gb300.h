@@ -44,7 +44,8 @@ typedef enum dp_status {
     DP_ERR_OOM = 5,         /* device memory or an admission budget exhausted */
     DP_ERR_UNSUPPORTED = 6, /* a scene outside this build's limits */
     DP_ERR_RANGE = 7,       /* step past the start, size mismatch, bad index */
-    DP_ERR_BUSY = 8         /* a request slot or arena region is in use */
+    DP_ERR_BUSY = 8,        /* a request slot or arena region is in use */
+    DP_ERR_NONFINITE = 9    /* a batch scene's field became NaN or infinite (is_finite, src/cpu.rs:707-713) */
 } dp_status;
 
 /* Message for the last error on the calling thread ("" when none). */
@@ -335,6 +336,7 @@ typedef struct dp_batch_options {
     uint32_t cells_per_lane; /* tile width 32·this for every scene (1, 2 or 4); 0 = per scene, least waste */
     uint32_t unit_planes;    /* z-planes per work unit; 0 = chosen when the work list is rebuilt:
                                 64 when the batch holds 16 units per SM at that depth, else 24 */
+    uint32_t skip_finite_check; /* nonzero: no per-scene NaN/infinity check after each chunk */
 } dp_batch_options;
 
 dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out);
@@ -351,6 +353,15 @@ dp_status dp_batch_remove(dp_batch *batch, uint64_t id);
 dp_status dp_batch_advance_chunk(dp_batch *batch, uint32_t *stepping);
 dp_status dp_batch_wait(dp_batch *batch, uint32_t timeout_ms);
 dp_status dp_batch_status(dp_batch *batch, uint64_t id, uint64_t *step, uint64_t *target);
+/* Per-scene failure (is_finite, src/cpu.rs:707-713, on the device): after
+ * every chunk each stepping scene's fields are checked for NaN and infinity.
+ * A scene found non-finite stops stepping within two chunks (its target
+ * becomes the steps issued for it, so dp_batch_status shows it finished);
+ * *fault then reads DP_ERR_NONFINITE and *at_step its step count when it
+ * stopped.  DP_OK (and 0) otherwise.  Does not wait: marks of chunks still
+ * running are taken by dp_batch_wait and by later chunks.  The other scenes
+ * run on unaffected. */
+dp_status dp_batch_fault(dp_batch *batch, uint64_t id, dp_status *fault, uint64_t *at_step);
 /* read_electric / read_magnetic / read_intensity of one scene, dense. */
 dp_status dp_batch_read_field(dp_batch *batch, uint64_t id, uint32_t field, float *host, size_t count);
 /* Probe series: step-major, then probe, then (Ez, Hy). */
@@ -409,6 +420,22 @@ typedef struct dp_tuning {
     uint32_t candidates;                                  /* plans timed */
 } dp_tuning;
 dp_status dp_sim_autotune(dp_sim *sim, uint32_t steps, dp_tuning *out);
+/* The plan the handle runs now (ms_per_step and candidates 0); every field
+ * 0 on the one-thread-per-cell path. */
+dp_status dp_sim_plan(const dp_sim *sim, dp_tuning *out);
+/* Tuned plans are kept per process, keyed by the grid's extent and the
+ * device's SM count: a simulation created later for a grid of that shape,
+ * with the plan fields of dp_options left at 0, starts from the tuned plan,
+ * and a batch scene of that shape (cells_per_lane 0) takes its tile width.
+ * Export writes the cache as text, one line per shape ("nx ny nz sms
+ * cells_per_lane tile_y ring_slots z_chunk ms_per_step"), into buf
+ * (capacity cap, NUL-terminated); *len gets the length it needs without the
+ * NUL, even when cap is too small (DP_ERR_RANGE then).  Import adds such
+ * lines (DP_ERR_INVALID at a malformed line or a tile shape this build
+ * lacks; the lines before it are kept), so tuning can outlive the process. */
+dp_status dp_tune_cache_export(char *buf, size_t cap, size_t *len);
+dp_status dp_tune_cache_import(const char *text);
+void dp_tune_cache_clear(void);
 
 /* ---- Probes and asynchronous read-back ----------------------------------
  * Probes record Ez and Hy at given cells after every step into a device ring

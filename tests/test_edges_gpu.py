@@ -226,3 +226,34 @@ def test_written_fields_read_back_and_step_like_the_oracle(extent, kernel, threa
     ref.advance_by(7)
     assert np.array_equal(bits(sim.read_electric()), bits(ref.read_electric())), extent
     assert np.array_equal(bits(sim.read_magnetic()), bits(ref.read_magnetic())), extent
+
+
+def test_a_tuned_plan_is_kept_for_its_grid_shape(threads):
+    """dp_sim_autotune remembers the plan it picked for the grid's extent: a
+    simulation created afterwards for a grid of that shape, with default
+    options, starts from it, and exported and re-imported text gives the
+    same plan; results stay bit-identical to the oracle either way."""
+    from tests import scenes
+    from diaphane_gb300.simulation import tuning_cache_clear, tuning_cache_export, tuning_cache_import
+    tuning_cache_clear()
+    scene, _ = scenes.graded()
+    sim = Simulation(scene, kernel=DP_KERNEL_FUSED)
+    sim.advance_by(5)
+    tuned = sim.autotune(steps=2)
+    plan = {k: tuned[k] for k in ("cells_per_lane", "tile_y", "ring_slots", "z_chunk")}
+    assert sim.plan() == plan
+    text = tuning_cache_export()
+    assert len(text.splitlines()) == 1
+    later = Simulation(scene, kernel=DP_KERNEL_FUSED)
+    assert later.plan() == plan
+    tuning_cache_clear()
+    assert tuning_cache_export() == ""
+    tuning_cache_import(text)
+    again = Simulation(scene, kernel=DP_KERNEL_FUSED)
+    assert again.plan() == plan
+    again.advance_by(20)
+    ref = oracle.OracleSimulation(scene, threads=threads)
+    ref.advance_by(20)
+    assert np.array_equal(bits(again.read_electric()), bits(ref.read_electric()))
+    assert np.array_equal(bits(again.read_magnetic()), bits(ref.read_magnetic()))
+    tuning_cache_clear()

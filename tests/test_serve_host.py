@@ -2,14 +2,16 @@
 fake batch and a fake clock.  Admission in arrival order while bytes and
 slots allow, waiting (not failing) on DP_ERR_OOM / DP_ERR_BUSY while another
 request can still leave, failing when nothing can, and each request leaving
-with its series at the chunk where its last step ran."""
+with its series at the chunk where its last step ran, a scene that the
+batch's finiteness check stopped retired as failed, and a request whose
+client gave up dropped from the queue or the batch as cancelled."""
 from types import SimpleNamespace
 
 import numpy as np
 import pytest
 
 import diaphane_gb300.serve as serve_mod
-from diaphane_gb300._abi import DP_ERR_BUSY, DP_ERR_OOM, DiaphaneError
+from diaphane_gb300._abi import DP_ERR_BUSY, DP_ERR_NONFINITE, DP_ERR_OOM, DiaphaneError
 from diaphane_gb300.serve import Request, Server, summary
 
 
@@ -28,10 +30,13 @@ class FakeClock:
 
 class FakeBatch:
     """Admission by bytes and slots, `chunk` steps per advance, a series of
-    the scene's id at every step."""
+    the scene's id at every step; a scene named in `blow_up` (name -> step)
+    is stopped by the finiteness check at the first chunk past that step."""
 
-    def __init__(self, slots, capacity, chunk=10):
+    def __init__(self, slots, capacity, chunk=10, blow_up=None):
         self.slots, self.capacity, self.chunk = slots, capacity, chunk
+        self.blow_up = blow_up or {}
+        self.faults = {}
         self.active = {}
         self.used = 0
         self.next_id = 0
@@ -44,18 +49,25 @@ class FakeBatch:
             raise DiaphaneError(DP_ERR_OOM, "the arena cannot hold this scene now")
         ident = self.next_id
         self.next_id += 1
-        self.active[ident] = [0, steps, resolved.bytes]
+        self.active[ident] = [0, steps, resolved.bytes, resolved.name]
         self.used += resolved.bytes
         self.log.append(("add", resolved.name))
         return ident
 
     def status(self, ident):
-        step, target, _ = self.active[ident]
+        step, target = self.active[ident][:2]
         return step, target
 
+    def fault(self, ident):
+        return self.faults.get(ident, (0, 0))
+
     def advance_chunk(self):
-        for entry in self.active.values():
+        for ident, entry in self.active.items():
             entry[0] = min(entry[1], entry[0] + self.chunk)
+            at = self.blow_up.get(entry[3])
+            if at is not None and entry[0] >= at and ident not in self.faults:
+                self.faults[ident] = (DP_ERR_NONFINITE, entry[0])
+                entry[1] = entry[0]  # stops stepping: looks finished
         return len(self.active)
 
     def wait(self, timeout_ms=0):
@@ -152,3 +164,34 @@ def test_idle_time_waits_for_the_next_arrival(monkeypatch):
     server.serve(trace)
     late = trace[1]
     assert late.admitted >= 5.0 and late.done >= late.admitted
+
+
+def test_a_failing_request_is_retired_as_failed_and_the_others_finish(monkeypatch):
+    clock = FakeClock()
+    batch = FakeBatch(slots=8, capacity=1 << 30, chunk=10, blow_up={1: 35})
+    server = make_server(batch, clock, monkeypatch)
+    trace = requests([(0.0, 200, 10), (0.0, 200, 10), (0.0, 120, 10)])
+    server.serve(trace)
+    assert trace[1].outcome == "failed" and trace[1].fault_step == 40 and trace[1].series is None
+    for r in (trace[0], trace[2]):
+        assert r.outcome == "done" and r.series.shape == (r.steps, 1, 2)
+    assert not batch.active and batch.used == 0
+    s = summary(trace)
+    assert s["solved"] == 2 and s["failed"] == 1 and s["cancelled"] == 0
+
+
+def test_a_client_that_gives_up_is_dropped_from_the_queue_or_the_batch(monkeypatch):
+    clock = FakeClock(tick=0.01)
+    batch = FakeBatch(slots=1, capacity=1 << 30, chunk=10)
+    server = make_server(batch, clock, monkeypatch)
+    # 0 runs long and gives up mid-run; 1 waits behind it for the one slot and
+    # gives up while queued; 2 is solved once 0 has left.
+    trace = requests([(0.0, 10_000, 1), (0.0, 10, 1), (0.0, 30, 1)])
+    trace[0].cancel_after = 0.5
+    trace[1].cancel_after = 0.2
+    server.serve(trace)
+    assert [r.outcome for r in trace] == ["cancelled", "cancelled", "done"]
+    assert trace[0].series is None and trace[1].series is None and trace[1].admitted is None
+    assert ("remove", 0) in batch.log and trace[0].done >= 0.5
+    assert not batch.active and batch.used == 0
+    assert summary(trace)["cancelled"] == 2
