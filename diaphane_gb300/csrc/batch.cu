@@ -553,14 +553,9 @@ struct dp_batch {
     }
 
     void wait(uint32_t timeout_ms) {
-        const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
-        for (;;) {
-            cudaError_t q = cudaStreamQuery(stream);
-            if (q == cudaSuccess) break;
-            if (q != cudaErrorNotReady) check(q, "stream");
-            if (std::chrono::steady_clock::now() >= deadline) throw Error(DP_ERR_TIMEOUT, "the batch did not finish in time");
-            std::this_thread::sleep_for(std::chrono::microseconds(50));
-        }
+        const cudaError_t q = poll_stream(stream, timeout_ms);
+        if (q == cudaErrorNotReady) throw Error(DP_ERR_TIMEOUT, "the batch did not finish in time");
+        check(q, "stream");
         collect_marks(-1);
         int32_t code = 0;
         check(cudaMemcpy(&code, error, sizeof(code), cudaMemcpyDeviceToHost), "error flag");

@@ -7,10 +7,30 @@
 // reference's f32 arithmetic (src/cpu.rs:283-434).
 #pragma once
 
+#include <chrono>
 #include <cstdint>
+#include <thread>
 #include <cuda_runtime.h>
 
 namespace diaphane {
+
+// Waits for a stream with a deadline: cudaSuccess when its work is done,
+// cudaErrorNotReady when `timeout_ms` passed first, or the stream's error.
+// The first 200 µs poll without sleeping, so a short wait (a field read, the
+// end of a chunk) returns within a few µs of the work; longer waits poll
+// every 50 µs.
+inline cudaError_t poll_stream(cudaStream_t stream, uint32_t timeout_ms) {
+    const auto start = std::chrono::steady_clock::now();
+    const auto spin = start + std::chrono::microseconds(200);
+    const auto deadline = start + std::chrono::milliseconds(timeout_ms);
+    for (;;) {
+        const cudaError_t q = cudaStreamQuery(stream);
+        if (q != cudaErrorNotReady) return q;
+        const auto now = std::chrono::steady_clock::now();
+        if (now >= deadline) return cudaErrorNotReady;
+        if (now >= spin) std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
 
 // Tables a step kernel reads.  All pointers are device pointers.
 struct DeviceScene {

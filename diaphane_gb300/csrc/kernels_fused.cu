@@ -41,6 +41,7 @@
 
 #include <cuda.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cstdio>
 #include <stdexcept>
@@ -86,12 +87,7 @@ template <int CX, int TY, int SLOTS> struct Geometry {
     static constexpr int SCRATCH_OFF = (BAR_OFF + kSlots * 8 + 15) & ~15;
     static constexpr int SCRATCH_WARP = 2 * kCompactItems * 4;
     static constexpr int INJ_OFF = SCRATCH_OFF + kWarps * SCRATCH_WARP; // 16-aligned
-    // The z-profile samples of a chunk's planes (magnetic gain, electric gain,
-    // absorber at the integer and the half position), one float4 per plane,
-    // for chunks of up to kZPlanes planes.
-    static constexpr int kZPlanes = 64;
-    static constexpr int ZP_OFF = (INJ_OFF + kMaxInjections * int(sizeof(DeviceInjection)) + 15) & ~15;
-    static constexpr int SMEM = ZP_OFF + kZPlanes * 16;
+    static constexpr int SMEM = INJ_OFF + kMaxInjections * int(sizeof(DeviceInjection));
 };
 
 struct FusedArgs {
@@ -437,18 +433,6 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         for (int p = zs; p <= min(zs + kSlots - 1, last_plane); ++p) issue(p);
     }
     for (int m = threadIdx.x; m < kMaxMaterials; m += kThreads) coeff[m] = __ldg(&s.coeff[m]);
-    // The chunk's z-profile samples, staged with the table: one shared load
-    // per plane instead of four dependent global ones.
-    float4 *zprof = reinterpret_cast<float4 *>(smem + G::ZP_OFF);
-    const bool zstaged = z1 - zs <= G::kZPlanes;
-    if (zstaged) {
-        const int off = int(s.n[0] + s.n[1]);
-        const float *ai = s.absorber, *ah = s.absorber + (s.n[0] + s.n[1] + s.n[2]);
-        for (int i = threadIdx.x; i < z1 - zs; i += kThreads) {
-            const int q = off + zs + i;
-            zprof[i] = make_float4(__ldg(&s.mgain[q]), __ldg(&s.egain[q]), __ldg(&ai[q]), __ldg(&ah[q]));
-        }
-    }
     {
         constexpr int kWords = int(sizeof(DeviceInjection) / 4);
         const uint32_t *from = reinterpret_cast<const uint32_t *>(u.inj.item);
@@ -565,14 +549,8 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         auto h_at = [&](float *base, int c, int r, int cc) { return base + (c * G::HR + r) * G::W + cc; };
 
         const bool prologue = p < z0;
-        float mgz, egz, aiz, ahz;
-        if (zstaged) {
-            const float4 zv = zprof[p - zs];
-            mgz = zv.x, egz = zv.y, aiz = zv.z, ahz = zv.w;
-        } else {
-            mgz = __ldg(&s.mgain[nx + ny + p]), egz = __ldg(&s.egain[nx + ny + p]);
-            aiz = __ldg(&absorb_int[nx + ny + p]), ahz = __ldg(&absorb_half[nx + ny + p]);
-        }
+        const float mgz = __ldg(&s.mgain[nx + ny + p]), egz = __ldg(&s.egain[nx + ny + p]);
+        const float aiz = __ldg(&absorb_int[nx + ny + p]), ahz = __ldg(&absorb_half[nx + ny + p]);
         const uint64_t at = (uint64_t(p) * ny + uint64_t(y)) * pitch + xl; // this lane's first cell
 
         // Intensity of this thread's cells, fetched early.
@@ -1019,11 +997,16 @@ FusedPlan fused_plan(const uint32_t n[3], uint32_t cx, uint32_t tile_y, uint32_t
     p.ctas_per_sm = uint32_t(resident_ctas(int(p.cx), int(p.tile_y), int(p.slots)));
     if (z_chunk == 0) {
         // Pick the chunk depth whose CTA count fills whole waves best, among
-        // depths of at least 16 planes (each chunk rebuilds one extra plane).
+        // depths of 16 to 32 planes (each chunk rebuilds one extra plane).
+        // Deeper chunks measured slower even where they fill the waves as
+        // well: at 384³ one wave of 192-plane chunks ran 0.829 ms a step
+        // against 0.644-0.670 ms for 20- to 32-plane chunks, reading 18 %
+        // more from DRAM (CTAs that walk far drift apart along z, and the
+        // halo rows a neighbour shares no longer meet in L2).
         const uint32_t resident = p.ctas_per_sm * uint32_t(sm_count > 0 ? sm_count : 1);
         double best = 1e30;
         z_chunk = n[2];
-        for (uint32_t depth = 16; depth <= n[2] + 15; ++depth) {
+        for (uint32_t depth = 16; depth <= std::min<uint32_t>(n[2] + 15, 32); ++depth) {
             const uint32_t chunks = (n[2] + depth - 1) / depth;
             const uint32_t waves = (tiles * chunks + resident - 1) / resident;
             const double cost = double(waves) * double(depth + 1);

@@ -224,14 +224,9 @@ struct dp_sim {
     }
 
     void wait(uint32_t timeout_ms) {
-        const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
-        for (;;) {
-            cudaError_t q = cudaStreamQuery(stream);
-            if (q == cudaSuccess) break;
-            if (q != cudaErrorNotReady) diaphane::check_cuda(q, "stream");
-            if (std::chrono::steady_clock::now() >= deadline) throw Error(DP_ERR_TIMEOUT, "the GPU did not finish in time");
-            std::this_thread::sleep_for(std::chrono::microseconds(50));
-        }
+        const cudaError_t q = poll_stream(stream, timeout_ms);
+        if (q == cudaErrorNotReady) throw Error(DP_ERR_TIMEOUT, "the GPU did not finish in time");
+        diaphane::check_cuda(q, "stream");
         if (kernel == DP_KERNEL_FUSED) {
             int32_t code = 0;
             diaphane::check_cuda(cudaMemcpy(&code, error, sizeof(code), cudaMemcpyDeviceToHost), "error flag");

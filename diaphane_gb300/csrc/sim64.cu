@@ -115,14 +115,9 @@ struct dp_sim64 {
     }
 
     void wait(uint32_t timeout_ms) {
-        const auto deadline = std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms);
-        for (;;) {
-            cudaError_t q = cudaStreamQuery(stream);
-            if (q == cudaSuccess) return;
-            if (q != cudaErrorNotReady) check(q, "stream");
-            if (std::chrono::steady_clock::now() >= deadline) throw Error(DP_ERR_TIMEOUT, "the GPU did not finish in time");
-            std::this_thread::sleep_for(std::chrono::microseconds(100));
-        }
+        const cudaError_t q = poll_stream(stream, timeout_ms);
+        if (q == cudaErrorNotReady) throw Error(DP_ERR_TIMEOUT, "the GPU did not finish in time");
+        check(q, "stream");
     }
 };
 

@@ -116,7 +116,7 @@ extern "C" dp_status dp_sim_autotune(dp_sim *sim, uint32_t steps, dp_tuning *out
         for (const Candidate &shape : shapes) {
             if (!fused_variant_exists(shape.cx, shape.ty, shape.slots)) continue;
             // The wave-filling depth the planner picks (0), and fixed depths.
-            for (uint32_t depth : {0u, 32u, 64u, 128u, n[2]}) {
+            for (uint32_t depth : {0u, 16u, 20u, 24u, 32u, 64u, 128u, n[2]}) {
                 if (depth > n[2]) continue;
                 Candidate c = shape;
                 c.z_chunk = depth;
