@@ -310,6 +310,7 @@ def run_ours(args):
         sim.wait(600_000)
         barrier()
     launches = sim.launch_count() - launches0
+    plan = sim.plan()
     ms = max_over_ranks(start.elapsed_time(end), world)
     seconds = ms / 1e3
     value = world * cells * args.steps / seconds / 1e9
@@ -398,7 +399,7 @@ def run_ours(args):
             "regime": {"timed_from_step": first_timed,
                        "what": f"{args.regime} untimed steps and {args.warmup} warm-up steps before the timed "
                                "window: the wave has crossed the box and the absorbers hold decaying field"},
-            "plan": sim.plan(), "tuned": tuned,
+            "plan": plan, "tuned": tuned,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks.summary(), "batched": batched, "served": served, "accuracy": accuracy}
     print(json.dumps(line), flush=True)
@@ -496,8 +497,11 @@ def default_accuracy(sim, resolved, device: int) -> dict:
     """FP64 error of the configurations the line stands for, on the GPU:
     the metric's 512³ scene at the step this run ended on (the f32 fields of
     the benchmarked simulation against the FP64 instance stepped as far),
-    free flight 80³ at 1000 steps normalized by the launched peak, and a
-    sample of the mixed-size batch's scenes at 1000 steps."""
+    free flight 80³ at 1000 steps normalized by the launched peak, the
+    graded stack 640×256×256 at its 5000 steps, the 192³ graded conducting
+    box's windowed energy drift over 20,000 steps in f32 and FP64, and a
+    sample of the mixed-size batch's scenes (the served stream's scenes are
+    drawn the same way) at 1000 steps."""
     from diaphane_gb300 import Simulation64, workloads
     steps = sim.step_count()
     f64 = Simulation64(resolved, device=device)
@@ -511,6 +515,8 @@ def default_accuracy(sim, resolved, device: int) -> dict:
               "normalization": "max |f32 - f64| over all three components / max |f64| at that step"}
     f64.close()
     return {"heterogeneous_512": metric, "free_flight_80": free_flight_accuracy(device),
+            "graded_stack": accuracy_case("graded stack 640x256x256", workloads.graded_stack(), 5000, device),
+            "graded_cavity_drift": drift_case(device),
             "batched_sample": [accuracy_case(f"mixed scene {k}", workloads.mixed_scene(BATCH_SEED + k), 1000, device)
                                for k in range(3)]}
 
