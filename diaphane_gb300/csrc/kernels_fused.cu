@@ -127,7 +127,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
 }
 
 // Waits for a phase of an mbarrier, but never forever.
+// The clock is read only once the first probe finds the phase incomplete,
+// so a plane that has already landed costs one try_wait.  A budget of 0 or
+// less gives up without probing.
 __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, long long budget) {
+    if (budget <= 0) return false;
+    if (mbar_try_wait(bar, parity)) return true;
     const long long start = clock64();
     while (!mbar_try_wait(bar, parity))
         if (clock64() - start > budget) return false;
