@@ -2,7 +2,8 @@
 
 The reference ships no golden vectors and its Rust toolchain is not available,
 so these — restated from the unit tests in src/grid.rs, src/material.rs,
-src/boundary.rs, src/source.rs, src/cpu.rs and src/timeline.rs — are what pin
+src/boundary.rs, src/source.rs, src/cpu.rs, src/scene.rs (its rasterization
+known answers) and src/timeline.rs — are what pin
 the oracle's restatement of the reference's algorithm.  Each test names the
 reference test it restates.
 """
@@ -446,6 +447,50 @@ def test_energy_density_sums_to_the_total_energy():
     summed = float(np.sum(volume * density.astype(np.float64)))
     total = sim.energy().total()
     assert abs(summed - total) < total * 1e-4
+
+
+# ---- src/scene.rs:511-568 (rasterization known answers) -----------------------------------
+# Each checked on the oracle's index and on the product's host raster.
+
+def index_tables(scene):
+    from diaphane_gb300 import ResolvedScene
+    ours = ResolvedScene(scene).table(_abi.DP_TABLE_MATERIAL_INDEX).astype(np.uint32)
+    theirs = oracle_sim(scene).table(_abi.DP_TABLE_MATERIAL_INDEX)
+    assert np.array_equal(ours, theirs)
+    n = (scene.grid.extent.x, scene.grid.extent.y, scene.grid.extent.z)
+    return lambda c: int(theirs[(c[2] * n[1] + c[1]) * n[0] + c[0]])
+
+
+def test_an_empty_scene_is_all_vacuum():
+    scene = Scene.empty(Extent.cube(24), 1e-3)
+    at = index_tables(scene)
+    assert all(at((x, y, z)) == MaterialTable.VACUUM for x in (0, 11, 23) for y in (0, 12, 23) for z in (0, 7, 23))
+
+
+def test_shapes_rasterize_and_later_ones_win():
+    # Conducting walls: the reference's raster needs no absorber, and a
+    # 10-cell one does not fit the 16-cell domain (resolution would refuse it).
+    scene = Scene.empty(Extent.cube(16), 1e-3).with_boundary(Boundary.PEC)
+    glass = scene.materials.push(Material.refractive(1.5))
+    metal = scene.materials.push(Material.PERFECT_CONDUCTOR)
+    scene.shapes.append(Shape.block((0.0, 0.0, 0.0), (8e-3, 8e-3, 8e-3), glass))
+    scene.shapes.append(Shape.sphere((0.0, 0.0, 0.0), 2e-3, metal))
+    at = index_tables(scene)
+    assert at((0, 0, 0)) == MaterialTable.VACUUM
+    assert at((5, 5, 5)) == glass
+    assert at((8, 8, 8)) == metal
+    assert at((11, 11, 11)) == glass
+
+
+def test_a_slab_spans_one_axis_only():
+    scene = Scene.empty(Extent.cube(12), 1e-3).with_boundary(Boundary.PEC)
+    glass = scene.materials.push(Material.refractive(2.0))
+    scene.shapes.append(Shape.slab(Axis.Y, -1.5e-3, 3e-3, glass))
+    at = index_tables(scene)
+    assert at((0, 4, 11)) == glass
+    assert at((11, 4, 0)) == glass
+    assert at((5, 2, 5)) == MaterialTable.VACUUM
+    assert at((5, 6, 5)) == MaterialTable.VACUUM
 
 
 # ---- src/timeline.rs:215-423 (the Python Timeline over the oracle) ----------------------
