@@ -168,16 +168,19 @@ __global__ void scan_finite(const BatchScene *scenes, const BatchUnit *units, ui
     const uint32_t set = (bs.parity + bs.steps) & 1u;
     const uint32_t ny = bs.s.n[1];
     const uint32_t width = min(tx, bs.s.n[0] - unit.x0), rows = min(8u, ny - unit.y0);
-    const uint32_t per_plane = width * rows, planes = unit.z1 - unit.z0;
-    const uint32_t items = 6u * planes * per_plane;
+    const uint32_t planes = unit.z1 - unit.z0, lines = 6u * planes * rows;
+    // Threads run along x (tx of them per row, coalesced); a block covers
+    // blockDim / tx rows of the unit at a time, (component, plane, row) major.
+    const uint32_t x = threadIdx.x % tx, step = blockDim.x / tx;
     bool bad = false;
-    for (uint32_t i = threadIdx.x; i < items; i += blockDim.x) {
-        const uint32_t within = i % per_plane, rest = i / per_plane;
-        const uint32_t z = unit.z0 + rest % planes, c = rest / planes;
-        const uint64_t at = (uint64_t(z) * ny + unit.y0 + within / width) * bs.s.pitch + unit.x0 + within % width;
-        const float *f = c < 3 ? bs.e[set] + uint64_t(c) * bs.s.cells : bs.h[set] + uint64_t(c - 3) * bs.s.cells;
-        bad = bad || !isfinite(f[at]);
-    }
+    if (x < width)
+        for (uint32_t q = threadIdx.x / tx; q < lines && !bad; q += step) {
+            const uint32_t c = q / (planes * rows), rest = q % (planes * rows);
+            const uint64_t at =
+                (uint64_t(unit.z0 + rest / rows) * ny + unit.y0 + rest % rows) * bs.s.pitch + unit.x0 + x;
+            const float *f = c < 3 ? bs.e[set] + uint64_t(c) * bs.s.cells : bs.h[set] + uint64_t(c - 3) * bs.s.cells;
+            bad = !isfinite(f[at]);
+        }
     if (__syncthreads_or(bad) && threadIdx.x == 0) marks[unit.scene] = 1;
 }
 
