@@ -168,18 +168,22 @@ __global__ void scan_finite(const BatchScene *scenes, const BatchUnit *units, ui
     const uint32_t set = (bs.parity + bs.steps) & 1u;
     const uint32_t ny = bs.s.n[1];
     const uint32_t width = min(tx, bs.s.n[0] - unit.x0), rows = min(8u, ny - unit.y0);
-    const uint32_t planes = unit.z1 - unit.z0, lines = 6u * planes * rows;
     // Threads run along x (tx of them per row, coalesced); a block covers
-    // blockDim / tx rows of the unit at a time, (component, plane, row) major.
+    // blockDim / tx rows at a time.  No early exit, so the loads of several
+    // planes are in flight at once.
     const uint32_t x = threadIdx.x % tx, step = blockDim.x / tx;
+    const uint64_t pitch = bs.s.pitch;
     bool bad = false;
     if (x < width)
-        for (uint32_t q = threadIdx.x / tx; q < lines && !bad; q += step) {
-            const uint32_t c = q / (planes * rows), rest = q % (planes * rows);
-            const uint64_t at =
-                (uint64_t(unit.z0 + rest / rows) * ny + unit.y0 + rest % rows) * bs.s.pitch + unit.x0 + x;
-            const float *f = c < 3 ? bs.e[set] + uint64_t(c) * bs.s.cells : bs.h[set] + uint64_t(c - 3) * bs.s.cells;
-            bad = !isfinite(f[at]);
+        for (uint32_t c = 0; c < 6; ++c) {
+            const float *f = (c < 3 ? bs.e[set] + uint64_t(c) * bs.s.cells : bs.h[set] + uint64_t(c - 3) * bs.s.cells) +
+                             unit.x0 + x;
+            for (uint32_t yy = threadIdx.x / tx; yy < rows; yy += step) {
+                const float *line = f + (uint64_t(unit.z0) * ny + unit.y0 + yy) * pitch;
+                const uint64_t plane = uint64_t(ny) * pitch;
+#pragma unroll 4
+                for (uint32_t z = 0; z < unit.z1 - unit.z0; ++z) bad |= !isfinite(__ldcs(line + z * plane));
+            }
         }
     if (__syncthreads_or(bad) && threadIdx.x == 0) marks[unit.scene] = 1;
 }
