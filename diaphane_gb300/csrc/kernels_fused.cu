@@ -572,16 +572,16 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
         // New H at this thread's cells, kept in registers for the E phase
         // (the other warps read it from the H slot).
         Vec<CX> kept_hx, kept_hy, kept_hz;
-        // Old E at this thread's cells, kept from the H phase on the 32-wide
-        // tiles (three registers there; the wider tiles read it again from
-        // the slot, their registers being spoken for).
+        // Old E at this thread's cells, kept from the H phase on the 32- and
+        // 64-wide tiles (3 and 6 registers; the 128-wide tile reads it again
+        // from the slot, its registers being spoken for).
         Vec<CX> kept_ex, kept_ey, kept_ez;
         // ---------------- H(p): this warp's row ----------------
         {
             const Vec<CX> ex = lds<CX>(e_at(E, 0, row, col)), ex_up = lds<CX>(e_at(E, 0, row + 1, col));
             const Vec<CX> ey = lds<CX>(e_at(E, 1, row, col)), ez = lds<CX>(e_at(E, 2, row, col));
             const Vec<CX> ez_up = lds<CX>(e_at(E, 2, row + 1, col));
-            if constexpr (CX == 1) {
+            if constexpr (CX <= 2) {
                 kept_ex = ex;
                 kept_ey = ey;
                 kept_ez = ez;
@@ -746,7 +746,7 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 }
             }
             Vec<CX> ex, ey, ez;
-            if constexpr (CX == 1) {
+            if constexpr (CX <= 2) {
                 ex = kept_ex;
                 ey = kept_ey;
                 ez = kept_ez;
