@@ -635,16 +635,23 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 }
             } else {
                 float n0[CX], n1[CX], n2[CX];
-                bool zero = true;
 #pragma unroll
                 for (int j = 0; j < CX; ++j) {
                     n0[j] = (1.0f - lx[j]) * nhx.v[j] - gain[j] * cx_[j];
                     n1[j] = (1.0f - ly[j]) * nhy.v[j] - gain[j] * cy_[j];
                     n2[j] = (1.0f - lz[j]) * nhz.v[j] - gain[j] * cz_[j];
-                    zero = zero && n0[j] == 0.0f && n1[j] == 0.0f && n2[j] == 0.0f;
                 }
-                if (__all_sync(0xffffffffu, zero)) {
-                    // A field the wave has not reached yet: ±0 / d = ±0.
+                // All numerators zero (a field the wave has not reached yet:
+                // ±0 / d = ±0)?  One vote on each lane's first value settles
+                // the common case, where the field is there.
+                bool zero = false;
+                if (__all_sync(0xffffffffu, n0[0] == 0.0f)) {
+                    zero = true;
+#pragma unroll
+                    for (int j = 0; j < CX; ++j) zero = zero && n0[j] == 0.0f && n1[j] == 0.0f && n2[j] == 0.0f;
+                    zero = __all_sync(0xffffffffu, zero);
+                }
+                if (zero) {
 #pragma unroll
                     for (int j = 0; j < CX; ++j) {
                         nhx.v[j] = n0[j];
@@ -788,16 +795,23 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 }
             } else {
                 float n0[CX], n1[CX], n2[CX];
-                bool zero = true;
 #pragma unroll
                 for (int j = 0; j < CX; ++j) {
                     n0[j] = (1.0f - lx[j]) * ex.v[j] + ecoef[j].x * cx_[j];
                     n1[j] = (1.0f - ly[j]) * ey.v[j] + ecoef[j].x * cy_[j];
                     n2[j] = (1.0f - lz[j]) * ez.v[j] + ecoef[j].x * cz_[j];
-                    zero = zero && n0[j] == 0.0f && n1[j] == 0.0f && n2[j] == 0.0f;
                 }
-                if (__all_sync(0xffffffffu, zero)) {
-                    // A field the wave has not reached yet: ±0 / d = ±0.
+                // All numerators zero (a field the wave has not reached yet:
+                // ±0 / d = ±0)?  One vote on each lane's first value settles
+                // the common case, where the field is there.
+                bool zero = false;
+                if (__all_sync(0xffffffffu, n0[0] == 0.0f)) {
+                    zero = true;
+#pragma unroll
+                    for (int j = 0; j < CX; ++j) zero = zero && n0[j] == 0.0f && n1[j] == 0.0f && n2[j] == 0.0f;
+                    zero = __all_sync(0xffffffffu, zero);
+                }
+                if (zero) {
 #pragma unroll
                     for (int j = 0; j < CX; ++j) {
                         nex.v[j] = n0[j];
