@@ -212,6 +212,26 @@ template <int CX> __device__ __forceinline__ void stg_row(float *p, const Vec<CX
         if (j < valid) __stcs(p + j, r.v[j]);
 }
 
+// The three components of a field at one lane's cells, one test of the row
+// end for all three.
+template <int CX>
+__device__ __forceinline__ void stg_row3(float *p, uint64_t stride, const Vec<CX> &a, const Vec<CX> &b,
+                                         const Vec<CX> &c, int valid) {
+    if (valid >= CX) {
+        stg<CX>(p, a);
+        stg<CX>(p + stride, b);
+        stg<CX>(p + 2 * stride, c);
+        return;
+    }
+#pragma unroll
+    for (int j = 0; j < CX; ++j)
+        if (j < valid) {
+            __stcs(p + j, a.v[j]);
+            __stcs(p + stride + j, b.v[j]);
+            __stcs(p + 2 * stride + j, c.v[j]);
+        }
+}
+
 // Profile or gain samples for CX consecutive cells along x; cells past the
 // end of the axis read as zero (they are never stored).  Scalar loads: the
 // sections of the packed tables need not be 16-byte aligned, and this runs
@@ -705,9 +725,7 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 sts<CX>(h_at(H, 1, row, col), nhy);
                 sts<CX>(h_at(H, 2, row, col), nhz);
                 if (store_row) {
-                    stg_row<CX>(u.h_out + at, nhx, full_lane);
-                    stg_row<CX>(u.h_out + cells + at, nhy, full_lane);
-                    stg_row<CX>(u.h_out + 2 * cells + at, nhz, full_lane);
+                    stg_row3<CX>(u.h_out + at, cells, nhx, nhy, nhz, full_lane);
                 }
             }
         }
@@ -862,9 +880,7 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
             }
             if (mask_e) apply_injections<CX>(inj, s.weights, mask_e, xl, y, p, ex, ey, ez);
             if (store_row) {
-                stg_row<CX>(u.e_out + at, ex, full_lane);
-                stg_row<CX>(u.e_out + cells + at, ey, full_lane);
-                stg_row<CX>(u.e_out + 2 * cells + at, ez, full_lane);
+                stg_row3<CX>(u.e_out + at, cells, ex, ey, ez, full_lane);
                 if (accumulate) {
 #pragma unroll
                     for (int j = 0; j < CX; ++j) {
