@@ -92,7 +92,7 @@ class dp_injection(C.Structure):
 class dp_batch_options(C.Structure):
     _fields_ = [("device", C.c_int32), ("chunk_steps", C.c_uint32), ("arena_bytes", C.c_uint64),
                 ("max_scenes", C.c_uint32), ("use_graphs", C.c_uint32), ("cells_per_lane", C.c_uint32),
-                ("unit_planes", C.c_uint32), ("skip_finite_check", C.c_uint32)]
+                ("unit_planes", C.c_uint32), ("skip_finite_check", C.c_uint32), ("axis_order", C.c_uint32)]
 
 
 class dp_options(C.Structure):

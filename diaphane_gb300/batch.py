@@ -18,9 +18,10 @@ from .simulation import ResolvedScene, _output
 
 class Batch:
     def __init__(self, arena_bytes: int, chunk_steps: int = 50, max_scenes: int = 256, device: int = 0,
-                 use_graphs: bool = True, cells_per_lane: int = 0, unit_planes: int = 0, check_finite: bool = True):
+                 use_graphs: bool = True, cells_per_lane: int = 0, unit_planes: int = 0, check_finite: bool = True,
+                 axis_order: int = 0):
         opts = _abi.dp_batch_options(device, chunk_steps, arena_bytes, max_scenes, int(use_graphs), cells_per_lane,
-                                     unit_planes, int(not check_finite))
+                                     unit_planes, int(not check_finite), axis_order)
         handle = C.c_void_p()
         _abi.check(_abi.lib().dp_batch_create(C.byref(opts), C.byref(handle)))
         self.handle = handle

@@ -92,7 +92,10 @@ class Arena {
 
 struct Variant {
     uint32_t cx, tile_y, slots;
-    bool operator==(const Variant &o) const { return cx == o.cx && tile_y == o.tile_y && slots == o.slots; }
+    uint32_t scene_x = 0; // stored axis holding the scenes' x
+    bool operator==(const Variant &o) const {
+        return cx == o.cx && tile_y == o.tile_y && slots == o.slots && scene_x == o.scene_x;
+    }
 };
 
 // The variant a grid shape runs: the requested tile width, or else the widest
@@ -112,11 +115,80 @@ Variant variant_for(uint32_t nx, uint32_t requested_cx) {
     return Variant{best, 8, best == 1 ? 4u : 3u};
 }
 
+// A scene's extents in axis order `order`: stored[i] = n[kBatchAxisOrders[order][i]].
+void stored_extent(const uint32_t n[3], uint32_t order, uint32_t out[3]) {
+    for (int i = 0; i < 3; ++i) out[i] = n[kBatchAxisOrders[order][i]];
+}
+
+// The stored axis holding scene axis a (the inverse of kBatchAxisOrders).
+uint32_t stored_axis(uint32_t order, uint32_t a) {
+    for (uint32_t i = 0; i < 3; ++i)
+        if (uint32_t(kBatchAxisOrders[order][i]) == a) return i;
+    return a;
+}
+
+// The odd permutations, whose scenes keep their gain tables negated.
+bool reverses_curls(uint32_t order) { return order >= 1 && order <= 3; }
+
+// The variant a scene stored in axis order `order` runs (stored extents
+// `m`): as variant_for, except that a scene whose x is not stored along x
+// takes 32-wide tiles, the only ones that group its loss by the scene's axes.
+// `ok` is false when a requested width rules the order out.
+Variant variant_in(const uint32_t m[3], uint32_t order, uint32_t requested_cx, bool &ok) {
+    ok = true;
+    const uint32_t scene_x = stored_axis(order, 0);
+    if (scene_x == 0) return variant_for(m[0], requested_cx);
+    ok = requested_cx == 0 || requested_cx == 1;
+    Variant v = variant_for(m[0], 1);
+    v.scene_x = scene_x;
+    return v;
+}
+
+// Cells a scene's units cover in axis order `order`: whole tiles of the
+// variant's width along x and of 8 rows along y, every plane along z;
+// UINT64_MAX when the order is ruled out.
+uint64_t tiled_cells(const uint32_t n[3], uint32_t order, uint32_t requested_cx) {
+    uint32_t m[3];
+    stored_extent(n, order, m);
+    bool ok = true;
+    const uint32_t tx = 32 * variant_in(m, order, requested_cx, ok).cx;
+    if (!ok) return UINT64_MAX;
+    return uint64_t((m[0] + tx - 1) / tx * tx) * ((m[1] + 7) / 8 * 8) * m[2];
+}
+
+// Whether a scene may be stored with its axes permuted: not when a source
+// carries apodization weights or a total-field box's side-face profiles,
+// which are laid out along the scene's own axes.
+bool permutable(const Scene &s) { return s.weights.empty() && !s.has_boxes(); }
+
+// The axis order a scene is stored in.  `requested` 0: the order whose tiles
+// cover the fewest cells (ties to the lower order; on 256 mixed scenes with
+// axes of 32-160 cells this covers 14 % fewer cells than the scenes' own
+// order); k in 1-6: order k-1 for every permutable scene, unless a requested
+// tile width rules it out.  The arithmetic does not depend on the order (the
+// kernel keeps the scene's operation order), so neither do the results.
+uint32_t order_for(const Scene &s, uint32_t requested, uint32_t requested_cx) {
+    if (!permutable(s)) return 0;
+    if (requested) return tiled_cells(s.grid.n, requested - 1, requested_cx) == UINT64_MAX ? 0 : requested - 1;
+    uint32_t best = 0;
+    uint64_t cells_best = tiled_cells(s.grid.n, 0, requested_cx);
+    for (uint32_t order = 1; order < 6; ++order) {
+        const uint64_t cells = tiled_cells(s.grid.n, order, requested_cx);
+        if (cells < cells_best) {
+            best = order;
+            cells_best = cells;
+        }
+    }
+    return best;
+}
+
 struct Entry {
     uint64_t id = 0;
     Scene scene;
     uint32_t slot = 0;            // index into the descriptor array
     Variant variant{};
+    uint32_t order = 0;           // axis order the scene is stored in
+    uint32_t n[3] = {0, 0, 0};    // its extents in that order
     uint32_t pitch = 0, material_pitch = 0;
     uint64_t cells_padded = 0;
     size_t offset = 0, bytes = 0; // arena block
@@ -138,7 +210,8 @@ struct ProbeSlot {
     uint32_t slot;      // scene descriptor index
     uint32_t k;         // probe number within the scene
     uint32_t probes;    // probes of that scene
-    uint32_t cell;      // padded linear index
+    uint32_t cell;      // padded linear index, in the scene's stored order
+    uint32_t ez, hy;    // the stored components holding the scene's Ez and Hy
     float *series;      // the scene's probe series
 };
 
@@ -149,8 +222,8 @@ __global__ void gather_probes(const BatchScene *scenes, const ProbeSlot *slots, 
     const BatchScene &bs = scenes[ps.slot];
     if (step >= bs.steps) return;
     const uint32_t out = (bs.parity + step + 1u) & 1u; // the set this step wrote
-    const float ez = bs.e[out][2 * bs.s.cells + ps.cell];
-    const float hy = bs.h[out][bs.s.cells + ps.cell];
+    const float ez = bs.e[out][ps.ez * bs.s.cells + ps.cell];
+    const float hy = bs.h[out][ps.hy * bs.s.cells + ps.cell];
     const uint64_t at = ((bs.step0 + step) * ps.probes + ps.k) * 2;
     ps.series[at] = ez;
     ps.series[at + 1] = hy;
@@ -188,6 +261,57 @@ __global__ void scan_finite(const BatchScene *scenes, const BatchUnit *units, ui
     if (__syncthreads_or(bad) && threadIdx.x == 0) marks[unit.scene] = 1;
 }
 
+// Scene coordinates of stored cell (x, y, z) in an axis order: the scene's
+// coordinate along axes.a[i] is the stored coordinate i.
+struct Axes {
+    uint32_t a[3];
+};
+
+// The material index in a scene's stored axis order, rows of out_pitch cells
+// (past the stored x extent: 0), from the scene's own index (rows of
+// in_pitch).  One thread per stored cell.
+__global__ void index_to_stored(const uint8_t *in, uint32_t in_pitch, uint32_t scene_ny, uint8_t *out,
+                                uint32_t out_pitch, uint32_t nx, uint32_t ny, uint64_t total, Axes axes) {
+    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const uint32_t x = uint32_t(i % out_pitch);
+    const uint64_t r = i / out_pitch;
+    const uint32_t y = uint32_t(r % ny), z = uint32_t(r / ny);
+    uint8_t v = 0;
+    if (x < nx) {
+        uint32_t q[3];
+        q[axes.a[0]] = x;
+        q[axes.a[1]] = y;
+        q[axes.a[2]] = z;
+        v = in[(uint64_t(q[2]) * scene_ny + q[1]) * in_pitch + q[0]];
+    }
+    out[i] = v;
+}
+
+// A stored field back in the scene's own order, dense: component c of scene
+// cell (x, y, z) is stored component comp.a[c] at the stored cell whose
+// coordinate i is the scene's coordinate along axes.a[i].  One thread per
+// output value.
+__global__ void field_from_stored(const float *stored, uint64_t stride, uint32_t pitch, uint32_t stored_ny, Axes axes,
+                                  Axes comp, uint32_t nx, uint32_t ny, uint64_t cells, uint64_t total, float *out) {
+    const uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+    if (i >= total) return;
+    const uint32_t c = uint32_t(i / cells);
+    const uint64_t cell = i % cells;
+    uint32_t q[3];
+    q[0] = uint32_t(cell % nx);
+    q[1] = uint32_t((cell / nx) % ny);
+    q[2] = uint32_t(cell / (uint64_t(nx) * ny));
+    const uint64_t at = (uint64_t(q[axes.a[2]]) * stored_ny + q[axes.a[1]]) * pitch + q[axes.a[0]];
+    out[i] = stored[comp.a[c] * stride + at];
+}
+
+Axes axes_of(uint32_t order) {
+    Axes a{};
+    for (int i = 0; i < 3; ++i) a.a[i] = uint32_t(kBatchAxisOrders[order][i]);
+    return a;
+}
+
 void make_units(Entry &e, uint32_t planes);
 
 } // namespace
@@ -198,6 +322,7 @@ struct dp_batch {
     uint32_t chunk = 50;
     uint32_t capacity = 0;        // scene slots
     uint32_t cells_per_lane = 0;  // forced tile width (0: per scene)
+    uint32_t axis_order = 0;      // forced axis order + 1 (0: per scene)
     uint32_t unit_planes = 24;    // z-planes per work unit
     bool unit_planes_set = false; // configured, rather than chosen per rebuild
     int sm_count = 1;
@@ -302,7 +427,7 @@ struct dp_batch {
         if (!unit_planes_set) {
             uint64_t deep_units = 0;
             for (auto &kv : entries) {
-                const uint32_t *n = kv.second.scene.grid.n;
+                const uint32_t *n = kv.second.n;
                 const uint32_t tx = 32 * kv.second.variant.cx, ty = kv.second.variant.tile_y;
                 deep_units += uint64_t((n[0] + tx - 1) / tx) * ((n[1] + ty - 1) / ty) * ((n[2] + 63) / 64);
             }
@@ -338,8 +463,8 @@ struct dp_batch {
             }
             lists[v].insert(lists[v].end(), e.units.begin(), e.units.end());
             for (uint32_t k = 0; k < e.probe_cells.size(); ++k)
-                probe_lists[v].push_back(
-                    ProbeSlot{e.slot, k, uint32_t(e.probe_cells.size()), e.probe_cells[k], e.probes});
+                probe_lists[v].push_back(ProbeSlot{e.slot, k, uint32_t(e.probe_cells.size()), e.probe_cells[k],
+                                                   stored_axis(e.order, 2), stored_axis(e.order, 1), e.probes});
         }
         std::vector<ProbeSlot> probes;
         probe_offset.clear();
@@ -395,8 +520,8 @@ struct dp_batch {
             cudaStream_t lane = lanes[v];
             check(cudaStreamWaitEvent(lane, fork, 0), "fork");
             for (uint32_t t = 0; t < chunk; ++t) {
-                launch_batch_step(variants[v].cx, variants[v].tile_y, variants[v].slots, scenes, units[v],
-                                  unit_counts[v], inj, cnt, prof, capacity, t, error, lane);
+                launch_batch_step(variants[v].cx, variants[v].tile_y, variants[v].slots, variants[v].scene_x,
+                                  scenes, units[v], unit_counts[v], inj, cnt, prof, capacity, t, error, lane);
                 ++launches;
                 if (probe_count_v[v]) {
                     gather_probes<<<(probe_count_v[v] + 255) / 256, 256, 0, lane>>>(
@@ -494,17 +619,20 @@ struct dp_batch {
                 for (const StepInjection &si : step_injections) {
                     if (si.value == 0.0f) continue;
                     if (n == kBatchInjections) throw Error(DP_ERR_UNSUPPORTED, "too many injections for a batch scene");
+                    // In the scene's stored axis order (a permuted scene
+                    // has neither weights nor box profiles).
                     DeviceInjection &d = row[n++];
-                    for (int a = 0; a < 3; ++a) {
-                        d.origin[a] = si.origin[a];
-                        d.extent[a] = si.extent[a];
+                    const int *axes = kBatchAxisOrders[e.order];
+                    for (int i = 0; i < 3; ++i) {
+                        d.origin[i] = si.origin[axes[i]];
+                        d.extent[i] = si.extent[axes[i]];
                     }
-                    d.component = si.component;
+                    d.component = stored_axis(e.order, si.component);
                     d.magnetic = si.magnetic;
                     d.value = si.value;
                     d.weight_offset = si.weight_offset;
                     d.profile_offset = si.profile_offset < 0 ? -1 : si.profile_offset + rebase;
-                    d.profile_axis = si.profile_axis;
+                    d.profile_axis = stored_axis(e.order, si.profile_axis);
                 }
                 hc[size_t(t) * capacity + e.slot] = n;
             }
@@ -588,14 +716,15 @@ struct Layout {
 // layout of such a scene reports SIZE_MAX bytes instead of a wrapped product.
 constexpr uint64_t kMaxProbeValues = uint64_t(1) << 40;
 
-Layout layout_of(const Scene &s, uint32_t probe_count, uint64_t steps) {
+Layout layout_of(const Scene &s, uint32_t order, uint32_t probe_count, uint64_t steps) {
     Layout l{};
     const uint64_t probe_values = uint64_t(probe_count) * 2;
     if (probe_values && steps > kMaxProbeValues / probe_values) {
         l.total = SIZE_MAX;
         return l;
     }
-    const uint32_t *n = s.grid.n;
+    uint32_t n[3];
+    stored_extent(s.grid.n, order, n);
     l.pitch = (n[0] + 3) / 4 * 4;
     l.material_pitch = (n[0] + 15) / 16 * 16;
     l.cells = uint64_t(l.pitch) * n[1] * n[2];
@@ -613,7 +742,7 @@ Layout layout_of(const Scene &s, uint32_t probe_count, uint64_t steps) {
 }
 
 void make_units(Entry &e, uint32_t planes) {
-    const uint32_t *n = e.scene.grid.n;
+    const uint32_t *n = e.n;
     const uint32_t tx = 32 * e.variant.cx, ty = e.variant.tile_y;
     const uint32_t tiles_x = (n[0] + tx - 1) / tx, tiles_y = (n[1] + ty - 1) / ty;
     // Units of `planes` planes (at least 8): enough to amortize a unit's
@@ -645,6 +774,8 @@ dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out) {
             opts->cells_per_lane != 4)
             throw Error(DP_ERR_INVALID, "cells_per_lane must be 0, 1, 2 or 4");
         b->cells_per_lane = opts->cells_per_lane;
+        if (opts->axis_order > 6) throw Error(DP_ERR_INVALID, "axis_order must be 0 (per scene) or 1-6");
+        b->axis_order = opts->axis_order;
         b->unit_planes = opts->unit_planes ? opts->unit_planes : 24;
         b->unit_planes_set = opts->unit_planes != 0;
         if (opts->arena_bytes == 0) throw Error(DP_ERR_INVALID, "arena_bytes must be positive");
@@ -696,7 +827,10 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         uint32_t slot = 0;
         while (slot < b->capacity && b->slot_used[slot]) ++slot;
         if (slot == b->capacity) throw Error(DP_ERR_BUSY, "every scene slot of the batch is in use");
-        const Layout l = layout_of(s, probe_count, steps);
+        const uint32_t order = order_for(s, b->axis_order, b->cells_per_lane);
+        uint32_t n[3];
+        stored_extent(s.grid.n, order, n);
+        const Layout l = layout_of(s, order, probe_count, steps);
         if (l.total == SIZE_MAX) throw Error(DP_ERR_OOM, "the probe series of this many steps fit no arena");
         size_t offset = 0;
         if (!b->arena.allocate(l.total, offset)) throw Error(DP_ERR_OOM, "the batch arena cannot hold this scene now");
@@ -706,10 +840,14 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         e.scene = s;
         e.lines = IncidentLines<float>(s);
         e.slot = slot;
-        e.variant = variant_for(s.grid.n[0], b->cells_per_lane);
+        e.order = order;
+        for (int a = 0; a < 3; ++a) e.n[a] = n[a];
+        bool width_ok = true; // order_for kept to the orders the requested width allows
+        e.variant = variant_in(n, order, b->cells_per_lane, width_ok);
         TunedPlan tuned{};
-        if (b->cells_per_lane == 0 && tuned_plan(s.grid.n, b->sm_count, tuned) && tuned.tile_y == 8)
-            e.variant = variant_for(s.grid.n[0], tuned.cx); // the tile width tuned for this shape
+        if (b->cells_per_lane == 0 && stored_axis(order, 0) == 0 && tuned_plan(n, b->sm_count, tuned) &&
+            tuned.tile_y == 8)
+            e.variant = variant_for(n[0], tuned.cx); // the tile width tuned for this shape
         e.pitch = l.pitch;
         e.material_pitch = l.material_pitch;
         e.cells_padded = l.cells;
@@ -742,20 +880,51 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         check(cudaMemsetAsync(b->arena_base + offset, 0, 4 * l.fields + l.intensity, st), "zero fields");
         check(cudaMemsetAsync(b->marks + slot, 0, sizeof(int32_t), st), "finite mark");
         e.joined = b->chunks_run;
-        rasterize_on_device(s, material, l.material_pitch, st);
+        if (order == 0) {
+            rasterize_on_device(s, material, l.material_pitch, st);
+        } else {
+            // Rasterized in the scene's own order, then laid out in the
+            // stored one.
+            const uint64_t scene_cells = uint64_t(s.grid.n[0]) * s.grid.n[1] * s.grid.n[2];
+            uint8_t *own = nullptr;
+            check(cudaMallocAsync(reinterpret_cast<void **>(&own), std::max<uint64_t>(1, scene_cells), st), "raster");
+            rasterize_on_device(s, own, s.grid.n[0], st);
+            const uint64_t total = uint64_t(l.material_pitch) * n[1] * n[2];
+            index_to_stored<<<unsigned((total + 255) / 256), 256, 0, st>>>(own, s.grid.n[0], s.grid.n[1], material,
+                                                                           l.material_pitch, n[0], n[1], total,
+                                                                           axes_of(order));
+            check(cudaGetLastError(), "index layout");
+            check(cudaFreeAsync(own, st), "raster");
+        }
         std::vector<float4> table(256, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         for (size_t m = 0; m < s.coefficients.size(); ++m)
             table[m] = make_float4(s.coefficients[m].electric_gain, s.coefficients[m].electric_loss,
                                    s.coefficients[m].magnetic_gain, s.coefficients[m].magnetic_loss);
         check(cudaMemcpyAsync(coeff, table.data(), table.size() * sizeof(float4), cudaMemcpyHostToDevice, st), "coeff");
-        check(cudaMemcpyAsync(mgain, s.magnetic_gains.data(), s.magnetic_gains.size() * 4, cudaMemcpyHostToDevice, st), "gains");
-        check(cudaMemcpyAsync(egain, s.electric_gains.data(), s.electric_gains.size() * 4, cudaMemcpyHostToDevice, st), "gains");
-        check(cudaMemcpyAsync(absorber, s.absorber.data(), s.absorber.size() * 4, cudaMemcpyHostToDevice, st), "absorber");
+        // The per-axis tables (x | y | z sections) in the stored order.
+        auto stored_axes = [&](const float *from, std::vector<float> &to) {
+            for (int i = 0; i < 3; ++i) {
+                const int a = kBatchAxisOrders[order][i];
+                to.insert(to.end(), from + s.axis_offset(a), from + s.axis_offset(a) + s.grid.n[a]);
+            }
+        };
+        const size_t span = size_t(s.grid.n[0]) + s.grid.n[1] + s.grid.n[2];
+        std::vector<float> mg, eg, ab;
+        stored_axes(s.magnetic_gains.data(), mg);
+        stored_axes(s.electric_gains.data(), eg);
+        if (reverses_curls(order))
+            for (std::vector<float> *g : {&mg, &eg})
+                for (float &v : *g) v = -v;
+        stored_axes(s.absorber.data(), ab);         // integer samples
+        stored_axes(s.absorber.data() + span, ab);  // half-cell samples
+        check(cudaMemcpyAsync(mgain, mg.data(), mg.size() * 4, cudaMemcpyHostToDevice, st), "gains");
+        check(cudaMemcpyAsync(egain, eg.data(), eg.size() * 4, cudaMemcpyHostToDevice, st), "gains");
+        check(cudaMemcpyAsync(absorber, ab.data(), ab.size() * 4, cudaMemcpyHostToDevice, st), "absorber");
         if (!s.weights.empty())
             check(cudaMemcpyAsync(weights, s.weights.data(), s.weights.size() * 4, cudaMemcpyHostToDevice, st), "weights");
         // No wait: copies from pageable memory return once staged, and every
         // later use of these buffers is ordered behind them on the stream.
-        for (int a = 0; a < 3; ++a) d.s.n[a] = s.grid.n[a];
+        for (int a = 0; a < 3; ++a) d.s.n[a] = n[a];
         d.s.pitch = l.pitch;
         d.s.cells = l.cells;
         d.s.material = nullptr; // the fused step reads the index through its tensor map
@@ -765,6 +934,7 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         d.s.absorber = absorber;
         d.s.weights = weights;
         d.intensity = e.accumulate ? intensity : nullptr;
+        d.scene_z = stored_axis(order, 2);
         try {
             batch_scene_maps(d, e.variant.cx, e.variant.tile_y, material, l.material_pitch);
         } catch (const std::exception &ex) {
@@ -777,7 +947,8 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
                 b->arena.release(offset, l.total);
                 throw Error(DP_ERR_RANGE, "probe outside the grid");
             }
-            e.probe_cells.push_back(uint32_t((uint64_t(c[2]) * s.grid.n[1] + c[1]) * l.pitch + c[0]));
+            const int *axes = kBatchAxisOrders[order];
+            e.probe_cells.push_back(uint32_t((uint64_t(c[axes[2]]) * n[1] + c[axes[1]]) * l.pitch + c[axes[0]]));
         }
         b->slot_used[slot] = 1;
         *id = e.id;
@@ -864,10 +1035,27 @@ dp_status dp_batch_read_field(dp_batch *b, uint64_t id, uint32_t field, float *h
         const float *src = field == DP_FIELD_ELECTRIC ? e.desc.e[current]
                            : field == DP_FIELD_MAGNETIC ? e.desc.h[current] : e.desc.intensity;
         if (field > DP_FIELD_INTENSITY) throw Error(DP_ERR_INVALID, "unknown field");
-        try {
-            copy_fields_out(host, src, n, e.pitch, e.cells_padded, components, b->stream);
-        } catch (const std::runtime_error &ex) {
-            throw Error(DP_ERR_CUDA, ex.what());
+        if (e.order != 0) {
+            // Gathered into the scene's own order on the device first.
+            float *dense = nullptr;
+            const uint64_t total = uint64_t(components) * cells;
+            check(cudaMallocAsync(reinterpret_cast<void **>(&dense), std::max<uint64_t>(1, total) * sizeof(float),
+                                  b->stream),
+                  "readback");
+            Axes comp{{0, 0, 0}};
+            if (components == 3)
+                for (uint32_t c = 0; c < 3; ++c) comp.a[c] = stored_axis(e.order, c);
+            field_from_stored<<<unsigned((total + 255) / 256), 256, 0, b->stream>>>(
+                src, e.cells_padded, e.pitch, e.n[1], axes_of(e.order), comp, n[0], n[1], cells, total, dense);
+            check(cudaGetLastError(), "readback layout");
+            check(cudaMemcpyAsync(host, dense, total * sizeof(float), cudaMemcpyDeviceToHost, b->stream), "readback");
+            check(cudaFreeAsync(dense, b->stream), "readback");
+        } else {
+            try {
+                copy_fields_out(host, src, n, e.pitch, e.cells_padded, components, b->stream);
+            } catch (const std::runtime_error &ex) {
+                throw Error(DP_ERR_CUDA, ex.what());
+            }
         }
         b->wait(kTimeoutMs);
         return DP_OK;
@@ -899,7 +1087,14 @@ dp_status dp_batch_memory(const dp_batch *b, uint64_t *used, uint64_t *capacity)
 }
 
 uint64_t dp_scene_batch_bytes(const dp_scene *scene, uint32_t probe_count, uint64_t steps) {
-    return scene ? layout_of(scene_of(scene), probe_count, steps).total : 0;
+    if (!scene) return 0;
+    // The most any axis order the batch may pick takes (rows are padded
+    // along the stored x, so the orders differ by a little).
+    const Scene &s = scene_of(scene);
+    size_t most = 0;
+    for (uint32_t order = 0; order < (permutable(s) ? 6u : 1u); ++order)
+        most = std::max(most, layout_of(s, order, probe_count, steps).total);
+    return most;
 }
 
 uint64_t dp_batch_launch_count(const dp_batch *b) { return b ? b->launches : 0; }

@@ -194,6 +194,7 @@ struct alignas(64) BatchScene {
     uint32_t parity;              // set that holds the fields at the chunk's first step
     uint32_t steps;               // steps this scene takes in the chunk (0: idle)
     uint64_t step0;               // the scene's step count at the chunk's first step
+    uint32_t scene_z;             // stored axis holding the scene's z (kBatchAxisOrders)
 };
 
 // One CTA's work: a tile of one scene through planes [z0, z1).
@@ -204,10 +205,19 @@ struct BatchUnit {
 // Tensor maps of one batch scene (fields and index with row pitches).
 void batch_scene_maps(BatchScene &scene, uint32_t cx, uint32_t tile_y, const uint8_t *material,
                       uint32_t material_pitch);
-// One launch per step over every unit of one kernel variant.
+// Axis orders a batch scene can be stored in: stored axis i (x, y, z) holds
+// the scene's axis kBatchAxisOrders[order][i].  Order 0 is the scene's own;
+// 1-3 exchange two axes (a scene in one of these has its gain tables stored
+// negated, which reverses every curl's subtraction), 4 and 5 rotate all
+// three.  Scenes whose x is not stored along x run on 32-wide tiles.
+constexpr int kBatchAxisOrders[6][3] = {{0, 1, 2}, {1, 0, 2}, {0, 2, 1}, {2, 1, 0}, {1, 2, 0}, {2, 0, 1}};
+
+// One launch per step over every unit of one kernel variant: tile shape,
+// ring depth, and the stored axis holding its scenes' x (1 and 2 for 32-wide
+// tiles only).
 // `profiles`: the chunk's total-field box profile values (device), which the
 // injections' profile offsets index; null when no scene of the batch has a box.
-void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, const BatchScene *scenes,
+void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, uint32_t scene_x, const BatchScene *scenes,
                        const BatchUnit *units, uint32_t unit_count, const DeviceInjection *injections,
                        const uint32_t *injection_counts, const float *profiles, uint32_t scene_count,
                        uint32_t step, int32_t *error, cudaStream_t stream);

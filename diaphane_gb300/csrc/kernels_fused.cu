@@ -254,6 +254,56 @@ __device__ __forceinline__ float h_full(float h, float loss, float gain, float c
     return exact_div((1.0f - loss) * h - gain * curl, 1.0f + loss);
 }
 
+// Axis orders.  A batch may store a scene with its axes permuted, so that the
+// axis that fills tile rows best runs along x (a 40 x 100 x 150-cell scene
+// wastes fewer lanes as 150 x 100 x 40): stored axis i holds the scene's axis
+// kBatchAxisOrders[order][i].  The step then performs the scene's own
+// operations on the same operands, so its results are the unpermuted run's
+// bit for bit:
+//  * the curl of component a is the difference term along a+1 minus the one
+//    along a+2 (src/cpu.rs:323-325, 423-424); an odd permutation reverses the
+//    cyclic order.  Such a scene's gain tables are stored negated: each term
+//    t becomes -t, and (-t1) - (-t2) equals t2 - t1 exactly, signed zeros
+//    included (x - y is x + (-y), and IEEE addition commutes);
+//  * the loss is (material + (absorber_y + absorber_z)) + absorber_x in the
+//    scene's axes (src/cpu.rs:326 with the row sum of
+//    src/boundary.rs:186-196): the kernel adds its two axes that are not the
+//    scene's x first (loss_of below; 32-wide tiles only, wider tiles being
+//    given scenes whose x is stored along x);
+//  * the intensity adds the squares of the scene's Ex and Ey, then Ez's
+//    (src/cpu.rs:186-194).
+// Nothing negates a field (a difference that cancels exactly is +0 in either
+// frame, so negated fields would not be exact).
+
+// The total loss of one cell component from the material's and the absorber
+// samples along the stored x (`lane`), y (`row`) and z (`plane`), the sample
+// along the scene's x (stored axis SCENE_X) added last.
+template <int SCENE_X> __device__ __forceinline__ float loss_of(float k, float lane, float row, float plane) {
+    if constexpr (SCENE_X == 0) return (k + (row + plane)) + lane;
+    else if constexpr (SCENE_X == 1) return (k + (lane + plane)) + row;
+    else return (k + (lane + row)) + plane;
+}
+
+// |E|² of one cell, the square of stored component `scene_z` (the scene's
+// Ez) added last.
+__device__ __forceinline__ float squares_of(float ex, float ey, float ez, uint32_t scene_z) {
+    float sum;
+    if (scene_z == 2) {
+        sum = ex * ex;
+        sum += ey * ey;
+        sum += ez * ez;
+    } else if (scene_z == 1) {
+        sum = ex * ex;
+        sum += ez * ez;
+        sum += ey * ey;
+    } else {
+        sum = ey * ey;
+        sum += ez * ez;
+        sum += ex * ex;
+    }
+    return sum;
+}
+
 // The division step of a warp in which only a few lanes hold lossy cells.
 // Those lanes put their 3·CX numerators and denominators in the warp's
 // scratch, all 32 lanes divide them (one item each per round), and each lossy
@@ -413,14 +463,20 @@ struct UnitArgs {
     int32_t *error;         // set when a wait gives up
     InjectionView inj;
     int x0, y0, z0, z1;     // tile origin and planes [z0, z1)
+    uint32_t scene_z = 2;   // stored axis holding the scene's z (batch scenes)
 };
 
 // The fused step for one (scene, tile, z-chunk) unit; every kernel below is
 // this function applied to a unit chosen from its block index.
-template <int CX, int TY, int SLOTS>
+//
+// SCENE_X: the stored axis holding the scene's x (0 but for batch scenes on
+// 32-wide tiles).  ANY_ORDER: the scene may be stored in any axis order (the
+// batch kernels), whose intensity order u.scene_z gives.
+template <int CX, int TY, int SLOTS, int SCENE_X = 0, bool ANY_ORDER = false>
 __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUtensorMap *h_map_p,
                                           const CUtensorMap *m_map_p, const UnitArgs &u) {
     using G = Geometry<CX, TY, SLOTS>;
+    static_assert(SCENE_X == 0 || (ANY_ORDER && CX == 1), "scenes with x stored elsewhere run 32-wide");
     constexpr int kWarps = G::kWarps, kThreads = G::kThreads, kSlots = G::kSlots;
     extern __shared__ __align__(128) unsigned char smem[];
     const DeviceScene &s = u.s;
@@ -640,9 +696,15 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 cx_[j] = mgy * (ez_up.v[j] - ez.v[j]) - mgz * (ey_next.v[j] - ey.v[j]);
                 cy_[j] = mgz * (ex_next.v[j] - ex.v[j]) - mgx.v[j] * (ezr - ez.v[j]);
                 cz_[j] = mgx.v[j] * (eyr - ey.v[j]) - mgy * (ex_up.v[j] - ex.v[j]);
-                lx[j] = (c.w + row_x) + aix.v[j];
-                ly[j] = (c.w + row_y) + ahx.v[j];
-                lz[j] = (c.w + row_z) + ahx.v[j];
+                if constexpr (SCENE_X == 0) {
+                    lx[j] = (c.w + row_x) + aix.v[j];
+                    ly[j] = (c.w + row_y) + ahx.v[j];
+                    lz[j] = (c.w + row_z) + ahx.v[j];
+                } else {
+                    lx[j] = loss_of<SCENE_X>(c.w, aix.v[j], ahy, ahz);
+                    ly[j] = loss_of<SCENE_X>(c.w, ahx.v[j], aiy, ahz);
+                    lz[j] = loss_of<SCENE_X>(c.w, ahx.v[j], ahy, aiz);
+                }
                 lossless = lossless && lx[j] == 0.0f && ly[j] == 0.0f && lz[j] == 0.0f;
             }
             const unsigned lossy_lanes = __ballot_sync(0xffffffffu, !lossless);
@@ -739,8 +801,8 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
             const float ez = *e_at(E, 2, hr, cc), ez_r = *e_at(E, 2, hr, cc + 1), ez_up = *e_at(E, 2, hr + 1, cc);
             const float4 c = coeff[M[hr * G::WM + cc + 12]];
             float nx_ = *h_at(H, 0, hr, cc), ny_ = *h_at(H, 1, hr, cc), nz_ = *h_at(H, 2, hr, cc);
-            const float lx = (c.w + (hc.ahy + ahz)) + hc.aix, ly = (c.w + (hc.aiy + ahz)) + hc.ahx;
-            const float lz = (c.w + (hc.ahy + aiz)) + hc.ahx;
+            const float lx = loss_of<SCENE_X>(c.w, hc.aix, hc.ahy, ahz), ly = loss_of<SCENE_X>(c.w, hc.ahx, hc.aiy, ahz);
+            const float lz = loss_of<SCENE_X>(c.w, hc.ahx, hc.ahy, aiz);
             const float cxh = hc.mgy * (ez_up - ez) - mgz * (ey_n - ey);
             const float cyh = mgz * (ex_n - ex) - hc.mgx * (ez_r - ez);
             const float czh = hc.mgx * (ey_r - ey) - hc.mgy * (ex_up - ex);
@@ -797,9 +859,15 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 cx_[j] = egy * (hz.v[j] - hz_dn.v[j]) - egz * (hy.v[j] - hy_prev.v[j]);
                 cy_[j] = egz * (hx.v[j] - hx_prev.v[j]) - egx.v[j] * (hz.v[j] - hzl);
                 cz_[j] = egx.v[j] * (hy.v[j] - hyl) - egy * (hx.v[j] - hx_dn.v[j]);
-                lx[j] = (ecoef[j].y + row_x) + ahx.v[j];
-                ly[j] = (ecoef[j].y + row_y) + aix.v[j];
-                lz[j] = (ecoef[j].y + row_z) + aix.v[j];
+                if constexpr (SCENE_X == 0) {
+                    lx[j] = (ecoef[j].y + row_x) + ahx.v[j];
+                    ly[j] = (ecoef[j].y + row_y) + aix.v[j];
+                    lz[j] = (ecoef[j].y + row_z) + aix.v[j];
+                } else {
+                    lx[j] = loss_of<SCENE_X>(ecoef[j].y, ahx.v[j], aiy, aiz);
+                    ly[j] = loss_of<SCENE_X>(ecoef[j].y, aix.v[j], ahy, aiz);
+                    lz[j] = loss_of<SCENE_X>(ecoef[j].y, aix.v[j], aiy, ahz);
+                }
                 lossless = lossless && lx[j] == 0.0f && ly[j] == 0.0f && lz[j] == 0.0f;
             }
             Vec<CX> nex, ney, nez;
@@ -884,10 +952,14 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
                 if (accumulate) {
 #pragma unroll
                     for (int j = 0; j < CX; ++j) {
-                        float sum = ex.v[j] * ex.v[j];
-                        sum += ey.v[j] * ey.v[j];
-                        sum += ez.v[j] * ez.v[j];
-                        inten.v[j] += sum;
+                        if constexpr (ANY_ORDER) {
+                            inten.v[j] += squares_of(ex.v[j], ey.v[j], ez.v[j], u.scene_z);
+                        } else {
+                            float sum = ex.v[j] * ex.v[j];
+                            sum += ey.v[j] * ey.v[j];
+                            sum += ez.v[j] * ez.v[j];
+                            inten.v[j] += sum;
+                        }
                     }
                     stg_row<CX>(u.intensity + at, inten, full_lane);
                 }
@@ -935,8 +1007,9 @@ fused_step(const __grid_constant__ CUtensorMap e_map, const __grid_constant__ CU
 
 // A batch: block b is unit b of this variant's work list.  Scene descriptors
 // (with their tensor maps) live in global memory; a scene that has finished
-// its steps for this chunk, or has left the batch, is skipped.
-template <int CX, int TY, int SLOTS>
+// its steps for this chunk, or has left the batch, is skipped.  Every scene
+// of the list has its x stored along axis SCENE_X.
+template <int CX, int TY, int SLOTS, int SCENE_X>
 __global__ void __launch_bounds__(32 * TY, resident_ctas(CX, TY, SLOTS))
 fused_batch_step(const BatchScene *__restrict__ scenes, const BatchUnit *__restrict__ units,
                  const DeviceInjection *__restrict__ injections, const uint32_t *__restrict__ injection_counts,
@@ -966,7 +1039,8 @@ fused_batch_step(const BatchScene *__restrict__ scenes, const BatchUnit *__restr
     u.y0 = int(unit.y0);
     u.z0 = int(unit.z0);
     u.z1 = int(unit.z1);
-    step_unit<CX, TY, SLOTS>(e_map, h_map, m_map, u);
+    u.scene_z = bs.scene_z;
+    step_unit<CX, TY, SLOTS, SCENE_X, true>(e_map, h_map, m_map, u);
 }
 
 // ---- host side ----------------------------------------------------------------
@@ -1153,26 +1227,29 @@ size_t fused_variant_smem(uint32_t cx, uint32_t tile_y, uint32_t slots) { return
 
 namespace {
 
-template <int CX, int TY, int SLOTS> void configure_batch_variant() {
-    cudaFuncSetAttribute(fused_batch_step<CX, TY, SLOTS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+template <int CX, int TY, int SLOTS, int SCENE_X> void configure_batch_variant() {
+    cudaFuncSetAttribute(fused_batch_step<CX, TY, SLOTS, SCENE_X>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          Geometry<CX, TY, SLOTS>::SMEM);
-    cudaFuncSetAttribute(fused_batch_step<CX, TY, SLOTS>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    cudaFuncSetAttribute(fused_batch_step<CX, TY, SLOTS, SCENE_X>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                         100);
 }
 
-template <int CX, int TY, int SLOTS>
+template <int CX, int TY, int SLOTS, int SCENE_X>
 void launch_batch_variant(const BatchScene *scenes, const BatchUnit *units, uint32_t unit_count,
                           const DeviceInjection *injections, const uint32_t *counts, const float *profiles,
                           uint32_t scene_count, uint32_t step, int32_t *error, cudaStream_t stream) {
-    fused_batch_step<CX, TY, SLOTS><<<unit_count, 32 * TY, Geometry<CX, TY, SLOTS>::SMEM, stream>>>(
+    fused_batch_step<CX, TY, SLOTS, SCENE_X><<<unit_count, 32 * TY, Geometry<CX, TY, SLOTS>::SMEM, stream>>>(
         scenes, units, injections, counts, profiles, scene_count, step, error);
 }
 
 } // namespace
 
 void configure_batch_kernels() {
-    configure_batch_variant<4, 8, 3>();
-    configure_batch_variant<2, 8, 3>();
-    configure_batch_variant<1, 8, 4>();
+    configure_batch_variant<4, 8, 3, 0>();
+    configure_batch_variant<2, 8, 3, 0>();
+    configure_batch_variant<1, 8, 4, 0>();
+    configure_batch_variant<1, 8, 4, 1>();
+    configure_batch_variant<1, 8, 4, 2>();
 }
 
 bool tensor_maps_available() { return encoder() != nullptr; }
@@ -1186,17 +1263,21 @@ void set_ring_wait_budget(long long cycles) {
     }
 }
 
-void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, const BatchScene *scenes,
+void launch_batch_step(uint32_t cx, uint32_t tile_y, uint32_t slots, uint32_t scene_x, const BatchScene *scenes,
                        const BatchUnit *units, uint32_t unit_count, const DeviceInjection *injections,
                        const uint32_t *injection_counts, const float *profiles, uint32_t scene_count,
                        uint32_t step, int32_t *error, cudaStream_t stream) {
     if (unit_count == 0) return;
-    if (cx == 4 && tile_y == 8 && slots == 3)
-        launch_batch_variant<4, 8, 3>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
-    else if (cx == 2 && tile_y == 8 && slots == 3)
-        launch_batch_variant<2, 8, 3>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
-    else if (cx == 1 && tile_y == 8 && slots == 4)
-        launch_batch_variant<1, 8, 4>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
+    if (cx == 4 && tile_y == 8 && slots == 3 && scene_x == 0)
+        launch_batch_variant<4, 8, 3, 0>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
+    else if (cx == 2 && tile_y == 8 && slots == 3 && scene_x == 0)
+        launch_batch_variant<2, 8, 3, 0>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
+    else if (cx == 1 && tile_y == 8 && slots == 4 && scene_x == 0)
+        launch_batch_variant<1, 8, 4, 0>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
+    else if (cx == 1 && tile_y == 8 && slots == 4 && scene_x == 1)
+        launch_batch_variant<1, 8, 4, 1>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
+    else if (cx == 1 && tile_y == 8 && slots == 4 && scene_x == 2)
+        launch_batch_variant<1, 8, 4, 2>(scenes, units, unit_count, injections, injection_counts, profiles, scene_count, step, error, stream);
     else
         throw std::runtime_error("no batch kernel variant with that tile shape and ring depth");
 }

@@ -337,6 +337,10 @@ typedef struct dp_batch_options {
     uint32_t unit_planes;    /* z-planes per work unit; 0 = chosen when the work list is rebuilt:
                                 64 when the batch holds 16 units per SM at that depth, else 24 */
     uint32_t skip_finite_check; /* nonzero: no per-scene NaN/infinity check after each chunk */
+    uint32_t axis_order; /* 0: each scene stored in the axis order whose tiles cover the fewest cells;
+                            k in 1-6: order k-1 of (xyz, yxz, xzy, zyx, yzx, zxy) for every scene
+                            (scenes with sheet or total-field-box sources keep xyz).  Results do not
+                            depend on it: reads and probes come back in the scene's own axes. */
 } dp_batch_options;
 
 dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out);
@@ -367,7 +371,8 @@ dp_status dp_batch_read_field(dp_batch *batch, uint64_t id, uint32_t field, floa
 /* Probe series: step-major, then probe, then (Ez, Hy). */
 dp_status dp_batch_read_probes(dp_batch *batch, uint64_t id, float *host, size_t count);
 dp_status dp_batch_memory(const dp_batch *batch, uint64_t *used, uint64_t *capacity);
-/* Arena bytes a scene would take (for admission control); UINT64_MAX when
+/* Arena bytes a scene would take (for admission control: the most of any
+ * axis order the batch may store it in); UINT64_MAX when
  * its probe series (probe_count x steps x 2 values) would exceed 2^40 values,
  * which no arena holds (dp_batch_add then returns DP_ERR_OOM). */
 uint64_t dp_scene_batch_bytes(const dp_scene *scene, uint32_t probe_count, uint64_t steps);
