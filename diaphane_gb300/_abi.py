@@ -167,6 +167,7 @@ SIGNATURES = [
     ("dp_batch_memory", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("dp_scene_batch_bytes", C.c_uint64, [_P, C.c_uint32, C.c_uint64]),
     ("dp_batch_launch_count", C.c_uint64, [_P]),
+    ("dp_batch_layout", C.c_int, [_P, C.c_uint64, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     ("dp_energy_noalloc", C.c_int, [_P, _P, C.c_uint32, _P, C.c_uint32, C.c_uint32, _P, C.c_uint32, _P, _P,
                                      C.POINTER(C.c_uint32), _P, _P]),
     ("dp_sim_kernel", C.c_uint32, [_P]),

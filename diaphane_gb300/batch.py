@@ -76,6 +76,13 @@ class Batch:
         _abi.check(_abi.lib().dp_batch_status(self.handle, ident, C.byref(step), C.byref(target)))
         return step.value, target.value
 
+    def layout(self, ident: int) -> tuple[int, int]:
+        """(axis order, tile width in cells) the batch stores a scene in;
+        order 0 is the scene's own (xyz), 1-5 are yxz, xzy, zyx, yzx, zxy."""
+        order, width = C.c_uint32(), C.c_uint32()
+        _abi.check(_abi.lib().dp_batch_layout(self.handle, ident, C.byref(order), C.byref(width)))
+        return order.value, width.value
+
     def fault(self, ident: int) -> tuple[int, int]:
         """(DP_OK, 0), or (DP_ERR_NONFINITE, the step count it stopped at)
         for a scene whose fields a per-chunk check found NaN or infinite:

@@ -1099,4 +1099,15 @@ uint64_t dp_scene_batch_bytes(const dp_scene *scene, uint32_t probe_count, uint6
 
 uint64_t dp_batch_launch_count(const dp_batch *b) { return b ? b->launches : 0; }
 
+dp_status dp_batch_layout(dp_batch *b, uint64_t id, uint32_t *axis_order, uint32_t *tile_width) {
+    return guarded([&] {
+        if (!b || !axis_order || !tile_width) throw Error(DP_ERR_INVALID, "null argument");
+        auto it = b->entries.find(id);
+        if (it == b->entries.end()) throw Error(DP_ERR_RANGE, "no such scene in the batch");
+        *axis_order = it->second.order;
+        *tile_width = 32 * it->second.variant.cx;
+        return DP_OK;
+    });
+}
+
 } // extern "C"

@@ -377,6 +377,10 @@ dp_status dp_batch_memory(const dp_batch *batch, uint64_t *used, uint64_t *capac
  * which no arena holds (dp_batch_add then returns DP_ERR_OOM). */
 uint64_t dp_scene_batch_bytes(const dp_scene *scene, uint32_t probe_count, uint64_t steps);
 uint64_t dp_batch_launch_count(const dp_batch *batch);
+/* How the batch stores a scene (no reference counterpart; diagnostics):
+ * its axis order (0-5: xyz, yxz, xzy, zyx, yzx, zxy, stored axis i holding
+ * the scene's axis named i-th) and the width of its tiles in cells. */
+dp_status dp_batch_layout(dp_batch *batch, uint64_t id, uint32_t *axis_order, uint32_t *tile_width);
 
 /* Field energy of caller-owned device arrays, allocating nothing.  No
  * counterpart in the reference: it exists for callers that cannot call

@@ -26,6 +26,9 @@ def test_a_mixed_batch_matches_each_scene_run_alone(graphs):
     resolved = mixed(12, 120)
     batch = Batch(ARENA, chunk_steps=16, max_scenes=16, use_graphs=graphs)
     ids = [batch.add(r, 120 - 7 * k, accumulate_intensity=(k % 2 == 0)) for k, r in enumerate(resolved)]
+    # Stored in the axis orders whose tiles cover the fewest cells: some of
+    # these scenes are permuted, and must come out the same.
+    assert any(batch.layout(ident)[0] != 0 for ident in ids)
     batch.run_to_completion()
     for k, (ident, r) in enumerate(zip(ids, resolved)):
         solo = Simulation(r, kernel=DP_KERNEL_NAIVE)
@@ -187,6 +190,10 @@ def test_every_axis_order_gives_each_scene_its_own_results(order):
 
     batch = Batch(ARENA, chunk_steps=16, max_scenes=8, axis_order=order)
     ids = [batch.add(r, steps, accumulate_intensity=True, probes=probes(r)) for r in resolved]
+    for ident in ids:
+        stored, width = batch.layout(ident)
+        assert stored == order - 1 and width in (32, 64, 128)
+        assert stored in (0, 2) or width == 32  # the scene's x elsewhere than x: 32-wide tiles
     batch.run_to_completion()
     for k, (ident, r) in enumerate(zip(ids, resolved)):
         solo = Simulation(r, kernel=DP_KERNEL_NAIVE)
