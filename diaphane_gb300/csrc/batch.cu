@@ -132,27 +132,29 @@ bool reverses_curls(uint32_t order) { return order >= 1 && order <= 3; }
 
 // The variant a scene stored in axis order `order` runs (stored extents
 // `m`): as variant_for, except that a scene whose x is not stored along x
-// takes 32-wide tiles, the only ones that group its loss by the scene's axes.
-// `ok` is false when a requested width rules the order out.
-Variant variant_in(const uint32_t m[3], uint32_t order, uint32_t requested_cx, bool &ok) {
-    ok = true;
+// takes 32-wide tiles, the only ones built to group its loss by the scene's
+// axes.
+Variant variant_in(const uint32_t m[3], uint32_t order, uint32_t requested_cx) {
     const uint32_t scene_x = stored_axis(order, 0);
     if (scene_x == 0) return variant_for(m[0], requested_cx);
-    ok = requested_cx == 0 || requested_cx == 1;
     Variant v = variant_for(m[0], 1);
     v.scene_x = scene_x;
     return v;
+}
+
+// Whether a requested tile width (0: none) allows axis order `order`.
+bool order_allowed(uint32_t order, uint32_t requested_cx) {
+    return stored_axis(order, 0) == 0 || requested_cx == 0 || requested_cx == 1;
 }
 
 // Cells a scene's units cover in axis order `order`: whole tiles of the
 // variant's width along x and of 8 rows along y, every plane along z;
 // UINT64_MAX when the order is ruled out.
 uint64_t tiled_cells(const uint32_t n[3], uint32_t order, uint32_t requested_cx) {
+    if (!order_allowed(order, requested_cx)) return UINT64_MAX;
     uint32_t m[3];
     stored_extent(n, order, m);
-    bool ok = true;
-    const uint32_t tx = 32 * variant_in(m, order, requested_cx, ok).cx;
-    if (!ok) return UINT64_MAX;
+    const uint32_t tx = 32 * variant_in(m, order, requested_cx).cx;
     return uint64_t((m[0] + tx - 1) / tx * tx) * ((m[1] + 7) / 8 * 8) * m[2];
 }
 
@@ -169,7 +171,7 @@ bool permutable(const Scene &s) { return s.weights.empty() && !s.has_boxes(); }
 // kernel keeps the scene's operation order), so neither do the results.
 uint32_t order_for(const Scene &s, uint32_t requested, uint32_t requested_cx) {
     if (!permutable(s)) return 0;
-    if (requested) return tiled_cells(s.grid.n, requested - 1, requested_cx) == UINT64_MAX ? 0 : requested - 1;
+    if (requested) return order_allowed(requested - 1, requested_cx) ? requested - 1 : 0;
     uint32_t best = 0;
     uint64_t cells_best = tiled_cells(s.grid.n, 0, requested_cx);
     for (uint32_t order = 1; order < 6; ++order) {
@@ -842,8 +844,7 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         e.slot = slot;
         e.order = order;
         for (int a = 0; a < 3; ++a) e.n[a] = n[a];
-        bool width_ok = true; // order_for kept to the orders the requested width allows
-        e.variant = variant_in(n, order, b->cells_per_lane, width_ok);
+        e.variant = variant_in(n, order, b->cells_per_lane);
         TunedPlan tuned{};
         if (b->cells_per_lane == 0 && stored_axis(order, 0) == 0 && tuned_plan(n, b->sm_count, tuned) &&
             tuned.tile_y == 8)
