@@ -53,7 +53,8 @@ def parse():
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--side", type=int, default=512, help="grid side (512 is the workload; smaller for checks)")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--variant", default="", help="fused kernel cx,tile_y,slots (default: tuned)")
+    p.add_argument("--variant", default="",
+                   help="fused kernel cx,tile_y,slots[,z_chunk] (default: tuned)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-batched", action="store_true", help="skip the mixed-size batch measurement")
     p.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
@@ -277,9 +278,9 @@ def run_ours(args):
 
     scene = workloads.heterogeneous(args.side)
     resolved = ResolvedScene(scene)
-    v = [int(t) for t in args.variant.split(",")] if args.variant else [0, 0, 0]
+    v = ([int(t) for t in args.variant.split(",")] if args.variant else []) + [0, 0, 0, 0]
     sim = Simulation(resolved, kernel=DP_KERNEL_AUTO, device=device, cells_per_lane=v[0], tile_y=v[1],
-                     ring_slots=v[2])
+                     ring_slots=v[2], z_chunk=v[3])
     sim.set_accumulate_intensity(True)
     stream = torch.cuda.ExternalStream(sim_stream(sim), device=device)
     cells = sim.cells
