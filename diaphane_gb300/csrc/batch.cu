@@ -835,7 +835,21 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         const Layout l = layout_of(s, order, probe_count, steps);
         if (l.total == SIZE_MAX) throw Error(DP_ERR_OOM, "the probe series of this many steps fit no arena");
         size_t offset = 0;
+        for (uint32_t k = 0; k < probe_count; ++k) {
+            const uint32_t *c = probes + 3 * k;
+            if (c[0] >= s.grid.n[0] || c[1] >= s.grid.n[1] || c[2] >= s.grid.n[2])
+                throw Error(DP_ERR_RANGE, "probe outside the grid");
+        }
         if (!b->arena.allocate(l.total, offset)) throw Error(DP_ERR_OOM, "the batch arena cannot hold this scene now");
+        // The block goes back to the arena if admission fails past this point.
+        struct Hold {
+            Arena &arena;
+            size_t offset, bytes;
+            bool kept = false;
+            ~Hold() {
+                if (!kept) arena.release(offset, bytes);
+            }
+        } hold{b->arena, offset, l.total};
         b->bind();
         Entry e;
         e.id = b->next_id++;
@@ -939,18 +953,14 @@ dp_status dp_batch_add(dp_batch *b, const dp_scene *scene, uint64_t steps, int32
         try {
             batch_scene_maps(d, e.variant.cx, e.variant.tile_y, material, l.material_pitch);
         } catch (const std::exception &ex) {
-            b->arena.release(offset, l.total);
             throw Error(DP_ERR_CUDA, ex.what());
         }
         for (uint32_t k = 0; k < probe_count; ++k) {
             const uint32_t *c = probes + 3 * k;
-            if (c[0] >= s.grid.n[0] || c[1] >= s.grid.n[1] || c[2] >= s.grid.n[2]) {
-                b->arena.release(offset, l.total);
-                throw Error(DP_ERR_RANGE, "probe outside the grid");
-            }
             const int *axes = kBatchAxisOrders[order];
             e.probe_cells.push_back(uint32_t((uint64_t(c[axes[2]]) * n[1] + c[axes[1]]) * l.pitch + c[axes[0]]));
         }
+        hold.kept = true;
         b->slot_used[slot] = 1;
         *id = e.id;
         b->entries.emplace(e.id, std::move(e));
