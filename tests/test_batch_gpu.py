@@ -115,6 +115,22 @@ def test_admission_refuses_what_the_arena_cannot_hold():
     assert np.array_equal(bits(big.read_electric(ident)), bits(solo.read_electric()))
 
 
+def test_a_refused_admission_leaves_the_arena_as_it_was():
+    from diaphane_gb300 import DiaphaneError
+    (r,) = mixed(1, 0, seed0=4100, hi=48)
+    batch = Batch(ARENA, chunk_steps=10, max_scenes=4)
+    ident = batch.add(r, 20)
+    used = batch.memory()[0]
+    with pytest.raises(DiaphaneError) as err:
+        batch.add(r, 20, probes=[(1, 1, 1), (r.extent[0], 0, 0)])  # the second probe lies outside
+    assert err.value.name == "DP_ERR_RANGE"
+    assert batch.memory()[0] == used
+    batch.run_to_completion()
+    solo = Simulation(r)
+    solo.advance_by(20)
+    assert np.array_equal(bits(batch.read_electric(ident)), bits(solo.read_electric()))
+
+
 def test_reads_into_a_caller_buffer_match_fresh_arrays():
     import torch
     resolved = mixed(3, 30)
