@@ -339,8 +339,10 @@ typedef struct dp_batch_options {
     uint32_t skip_finite_check; /* nonzero: no per-scene NaN/infinity check after each chunk */
     uint32_t axis_order; /* 0: each scene stored in the axis order whose tiles cover the fewest cells;
                             k in 1-6: order k-1 of (xyz, yxz, xzy, zyx, yzx, zxy) for every scene
-                            (scenes with sheet or total-field-box sources keep xyz).  Results do not
-                            depend on it: reads and probes come back in the scene's own axes. */
+                            (scenes with sheet or total-field-box sources keep xyz, and so does a scene
+                            whose order would move its x off the stored x while cells_per_lane asks
+                            for 64- or 128-wide tiles).  Results do not depend on it: reads and
+                            probes come back in the scene's own axes. */
 } dp_batch_options;
 
 dp_status dp_batch_create(const dp_batch_options *opts, dp_batch **out);
