@@ -52,7 +52,8 @@ __device__ __forceinline__ uint32_t material_of(const DeviceScene &s, uint64_t i
 }
 
 // One injection of one step (Injection, src/source.rs:409-427).
-struct DeviceInjection {
+// 16-byte aligned so the step reads it as three 16-byte words.
+struct alignas(16) DeviceInjection {
     uint32_t origin[3];
     uint32_t extent[3];
     uint32_t component;
@@ -65,6 +66,7 @@ struct DeviceInjection {
     int32_t profile_offset;
     uint32_t profile_axis;
 };
+static_assert(sizeof(DeviceInjection) == 48, "three 16-byte words");
 
 // Non-silent injections of one step, in the reference's application order.
 constexpr int kMaxInjections = 32;

@@ -382,22 +382,28 @@ __device__ __forceinline__ void apply_injections(const InjectionView &t, const f
         const int k = __ffs(mask) - 1;
         mask &= mask - 1;
         const DeviceInjection &d = t.item[k];
-        const int dz = z - int(d.origin[2]);
-        if (dz < 0 || dz >= int(d.extent[2])) continue;
-        const int dy = y - int(d.origin[1]);
-        if (d.weight_offset < 0 && d.profile_offset < 0) {
+        // The descriptor as three 16-byte words: (origin x, y, z, extent x),
+        // (extent y, z, component, magnetic), (value, weight and profile
+        // offsets, profile axis).
+        const int4 w0 = reinterpret_cast<const int4 *>(&d)[0];
+        const int4 w1 = reinterpret_cast<const int4 *>(&d)[1];
+        const int4 w2 = reinterpret_cast<const int4 *>(&d)[2];
+        const int dz = z - w0.z;
+        if (dz < 0 || dz >= w1.y) continue;
+        const int dy = y - w0.y;
+        if (w2.y < 0 && w2.z < 0) {
             // Weight 1 everywhere (a point, a plane, a box's uniform face):
             // value * 1 is value, so each covered cell just adds it.
-            const int dx0 = x - int(d.origin[0]);
-            const uint32_t ex = d.extent[0];
-            const float add = d.value;
+            const int dx0 = x - w0.x;
+            const uint32_t ex = uint32_t(w0.w);
+            const float add = __int_as_float(w2.x);
             // The component is the injection's, the same on every lane: one
             // branch, then selects (not an added zero: -0 + 0 would turn a
             // cell's -0 into +0).
-            if (d.component == 0) {
+            if (w1.z == 0) {
 #pragma unroll
                 for (int j = 0; j < CX; ++j) f0.v[j] = uint32_t(dx0 + j) < ex ? f0.v[j] + add : f0.v[j];
-            } else if (d.component == 1) {
+            } else if (w1.z == 1) {
 #pragma unroll
                 for (int j = 0; j < CX; ++j) f1.v[j] = uint32_t(dx0 + j) < ex ? f1.v[j] + add : f1.v[j];
             } else {
