@@ -364,10 +364,11 @@ __device__ __forceinline__ uint32_t injection_mask(const InjectionView &t, bool 
                                                    int za, int zb) {
     uint32_t m = 0;
     for (uint32_t k = 0; k < t.count; ++k) {
-        const DeviceInjection &d = t.item[k];
-        if (d.magnetic == uint32_t(magnetic) && y >= int(d.origin[1]) && y < int(d.origin[1] + d.extent[1]) &&
-            xb > int(d.origin[0]) && xa < int(d.origin[0] + d.extent[0]) && zb > int(d.origin[2]) &&
-            za < int(d.origin[2] + d.extent[2]))
+        // (origin x, y, z, extent x), (extent y, z, component, magnetic)
+        const int4 w0 = reinterpret_cast<const int4 *>(&t.item[k])[0];
+        const int4 w1 = reinterpret_cast<const int4 *>(&t.item[k])[1];
+        if (w1.w == int(magnetic) && y >= w0.y && y < w0.y + w1.x && xb > w0.x && xa < w0.x + w0.w &&
+            zb > w0.z && za < w0.z + w1.y)
             m |= 1u << k;
     }
     return m;
@@ -553,10 +554,11 @@ __device__ __forceinline__ void step_unit(const CUtensorMap *e_map_p, const CUte
     // Both phases' masks in one pass over the table.
     uint32_t mask_h = 0, mask_e = 0;
     for (uint32_t k = 0; k < inj.count; ++k) {
-        const DeviceInjection &d = inj.item[k];
-        if (y >= int(d.origin[1]) && y < int(d.origin[1] + d.extent[1]) && xl + CX > int(d.origin[0]) &&
-            xl < int(d.origin[0] + d.extent[0]) && z1 > int(d.origin[2]) && zs < int(d.origin[2] + d.extent[2])) {
-            if (d.magnetic) mask_h |= 1u << k;
+        // (origin x, y, z, extent x), (extent y, z, component, magnetic)
+        const int4 w0 = reinterpret_cast<const int4 *>(&inj.item[k])[0];
+        const int4 w1 = reinterpret_cast<const int4 *>(&inj.item[k])[1];
+        if (y >= w0.y && y < w0.y + w1.x && xl + CX > w0.x && xl < w0.x + w0.w && z1 > w0.z && zs < w0.z + w1.y) {
+            if (w1.w) mask_h |= 1u << k;
             else mask_e |= 1u << k;
         }
     }
